@@ -1,0 +1,438 @@
+/* libawkward_gb300: GB300 (sm_103a) kernels for awkward's jagged hot path.
+ *
+ * Generated by awkward_gb300/gen_signatures.py from awkward's
+ * kernel-specification.yml; do not edit by hand.
+ *
+ * Every entry point keeps the name and the argument list of one
+ * specialization of kernel-specification.yml (cited per declaration as
+ * kernel-specification.yml:<line>, with the awkward-cpp CPU template it
+ * replaces), so a ctypes adapter can install it into awkward's cupy
+ * kernel table keyed by (family, *dtypes).  Differences from the spec:
+ *   - every pointer is a DEVICE pointer; List[List[T]] is a device array
+ *     of device pointers;
+ *   - three trailing arguments follow the spec's arguments:
+ *       uint64_t  invocation_index  index of this call in the caller's
+ *                                   pending-invocation list;
+ *       uint64_t* err_code          device word; a failing kernel does
+ *                                   atomicMin(err_code,
+ *                                     invocation_index*256 + message)
+ *                                   (awkward's RawModule protocol) and
+ *                                   kernels skip work when it is set;
+ *       void*     stream            cudaStream_t to launch on (0 = legacy).
+ *   - the return value is the cudaError_t of the launch (0 = success);
+ *     data errors are reported only through err_code.
+ * Outputs are preallocated by the caller.  Temporary buffers (tile
+ * states of the single-pass scans) come from a stream-ordered pool owned
+ * by the library and are released in stream order.
+ */
+#ifndef AWKWARD_GB300_H_
+#define AWKWARD_GB300_H_
+
+#include <stdint.h>
+#include <stdbool.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define AWKWARD_GB300_ERROR_BITS 8
+#define AWKWARD_GB300_NO_ERROR 0xffffffffffffffffULL
+
+/* ---- awkward_ListArray_combinations: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_combinations.cpp:9 */
+/* kernel-specification.yml:1127 */
+int awkward_ListArray32_combinations_64(int64_t** tocarry, int64_t* toindex, int64_t* fromindex, int64_t n, bool replacement, const int32_t* starts, const int32_t* stops, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1137 */
+int awkward_ListArray64_combinations_64(int64_t** tocarry, int64_t* toindex, int64_t* fromindex, int64_t n, bool replacement, const int64_t* starts, const int64_t* stops, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1147 */
+int awkward_ListArrayU32_combinations_64(int64_t** tocarry, int64_t* toindex, int64_t* fromindex, int64_t n, bool replacement, const uint32_t* starts, const uint32_t* stops, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListArray_combinations_length: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_combinations_length.cpp:8 */
+/* kernel-specification.yml:1177 */
+int awkward_ListArray32_combinations_length_64(int64_t* totallen, int64_t* tooffsets, int64_t n, bool replacement, const int32_t* starts, const int32_t* stops, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1186 */
+int awkward_ListArray64_combinations_length_64(int64_t* totallen, int64_t* tooffsets, int64_t n, bool replacement, const int64_t* starts, const int64_t* stops, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1195 */
+int awkward_ListArrayU32_combinations_length_64(int64_t* totallen, int64_t* tooffsets, int64_t n, bool replacement, const uint32_t* starts, const uint32_t* stops, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListArray_getitem_jagged_apply: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_getitem_jagged_apply.cpp:8 */
+/* kernel-specification.yml:1318 */
+int awkward_ListArray32_getitem_jagged_apply_64(int64_t* tooffsets, int64_t* tocarry, const int64_t* slicestarts, const int64_t* slicestops, int64_t sliceouterlen, const int64_t* sliceindex, int64_t sliceinnerlen, const int32_t* fromstarts, const int32_t* fromstops, int64_t contentlen, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1330 */
+int awkward_ListArray64_getitem_jagged_apply_64(int64_t* tooffsets, int64_t* tocarry, const int64_t* slicestarts, const int64_t* slicestops, int64_t sliceouterlen, const int64_t* sliceindex, int64_t sliceinnerlen, const int64_t* fromstarts, const int64_t* fromstops, int64_t contentlen, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1342 */
+int awkward_ListArrayU32_getitem_jagged_apply_64(int64_t* tooffsets, int64_t* tocarry, const int64_t* slicestarts, const int64_t* slicestops, int64_t sliceouterlen, const int64_t* sliceindex, int64_t sliceinnerlen, const uint32_t* fromstarts, const uint32_t* fromstops, int64_t contentlen, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListArray_getitem_jagged_carrylen: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_getitem_jagged_carrylen.cpp:8 */
+/* kernel-specification.yml:1398 */
+int awkward_ListArray_getitem_jagged_carrylen_64(int64_t* carrylen, const int64_t* slicestarts, const int64_t* slicestops, int64_t sliceouterlen, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListArray_getitem_jagged_descend: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_getitem_jagged_descend.cpp:8 */
+/* kernel-specification.yml:1416 */
+int awkward_ListArray32_getitem_jagged_descend_64(int64_t* tooffsets, const int64_t* slicestarts, const int64_t* slicestops, int64_t sliceouterlen, const int32_t* fromstarts, const int32_t* fromstops, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1424 */
+int awkward_ListArray64_getitem_jagged_descend_64(int64_t* tooffsets, const int64_t* slicestarts, const int64_t* slicestops, int64_t sliceouterlen, const int64_t* fromstarts, const int64_t* fromstops, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1432 */
+int awkward_ListArrayU32_getitem_jagged_descend_64(int64_t* tooffsets, const int64_t* slicestarts, const int64_t* slicestops, int64_t sliceouterlen, const uint32_t* fromstarts, const uint32_t* fromstops, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListArray_getitem_jagged_expand: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_getitem_jagged_expand.cpp:8 */
+/* kernel-specification.yml:1461 */
+int awkward_ListArray32_getitem_jagged_expand_64(int64_t* multistarts, int64_t* multistops, const int64_t* singleoffsets, int64_t* tocarry, const int32_t* fromstarts, const int32_t* fromstops, int64_t jaggedsize, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1471 */
+int awkward_ListArray64_getitem_jagged_expand_64(int64_t* multistarts, int64_t* multistops, const int64_t* singleoffsets, int64_t* tocarry, const int64_t* fromstarts, const int64_t* fromstops, int64_t jaggedsize, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1481 */
+int awkward_ListArrayU32_getitem_jagged_expand_64(int64_t* multistarts, int64_t* multistops, const int64_t* singleoffsets, int64_t* tocarry, const uint32_t* fromstarts, const uint32_t* fromstops, int64_t jaggedsize, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListArray_getitem_jagged_numvalid: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_getitem_jagged_numvalid.cpp:8 */
+/* kernel-specification.yml:1518 */
+int awkward_ListArray_getitem_jagged_numvalid_64(int64_t* numvalid, const int64_t* slicestarts, const int64_t* slicestops, int64_t length, const int64_t* missing, int64_t missinglength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListArray_getitem_jagged_shrink: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_getitem_jagged_shrink.cpp:8 */
+/* kernel-specification.yml:1547 */
+int awkward_ListArray_getitem_jagged_shrink_64(int64_t* tocarry, int64_t* tosmalloffsets, int64_t* tolargeoffsets, const int64_t* slicestarts, const int64_t* slicestops, int64_t length, const int64_t* missing, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListArray_getitem_next_range: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_getitem_next_range.cpp:9 */
+/* kernel-specification.yml:1741 */
+int awkward_ListArray32_getitem_next_range_64(int32_t* tooffsets, int64_t* tocarry, const int32_t* fromstarts, const int32_t* fromstops, int64_t lenstarts, int64_t start, int64_t stop, int64_t step, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1751 */
+int awkward_ListArray64_getitem_next_range_64(int64_t* tooffsets, int64_t* tocarry, const int64_t* fromstarts, const int64_t* fromstops, int64_t lenstarts, int64_t start, int64_t stop, int64_t step, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1761 */
+int awkward_ListArrayU32_getitem_next_range_64(uint32_t* tooffsets, int64_t* tocarry, const uint32_t* fromstarts, const uint32_t* fromstops, int64_t lenstarts, int64_t start, int64_t stop, int64_t step, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListArray_getitem_next_range_carrylength: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_getitem_next_range_carrylength.cpp:9 */
+/* kernel-specification.yml:1806 */
+int awkward_ListArray32_getitem_next_range_carrylength(int64_t* carrylength, const int32_t* fromstarts, const int32_t* fromstops, int64_t lenstarts, int64_t start, int64_t stop, int64_t step, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1815 */
+int awkward_ListArray64_getitem_next_range_carrylength(int64_t* carrylength, const int64_t* fromstarts, const int64_t* fromstops, int64_t lenstarts, int64_t start, int64_t stop, int64_t step, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1824 */
+int awkward_ListArrayU32_getitem_next_range_carrylength(int64_t* carrylength, const uint32_t* fromstarts, const uint32_t* fromstops, int64_t lenstarts, int64_t start, int64_t stop, int64_t step, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListArray_localindex: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_localindex.cpp:8 */
+/* kernel-specification.yml:1921 */
+int awkward_ListArray32_localindex_64(int64_t* toindex, const int32_t* offsets, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1926 */
+int awkward_ListArray64_localindex_64(int64_t* toindex, const int64_t* offsets, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1931 */
+int awkward_ListArrayU32_localindex_64(int64_t* toindex, const uint32_t* offsets, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_NumpyArray_reduce_adjust_starts_64: replaces awkward-cpp/src/cpu-kernels/awkward_NumpyArray_reduce_adjust_starts_64.cpp:7 */
+/* kernel-specification.yml:2552 */
+int awkward_NumpyArray_reduce_adjust_starts_64(int64_t* toptr, int64_t outlength, const int64_t* offsets, const int64_t* starts, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_NumpyArray_reduce_mask_ByteMaskedArray_64: replaces awkward-cpp/src/cpu-kernels/awkward_NumpyArray_reduce_mask_ByteMaskedArray_64.cpp:7 */
+/* kernel-specification.yml:2587 */
+int awkward_NumpyArray_reduce_mask_ByteMaskedArray_64(int8_t* toptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_RegularArray_getitem_jagged_expand: replaces awkward-cpp/src/cpu-kernels/awkward_RegularArray_getitem_jagged_expand.cpp:8 */
+/* kernel-specification.yml:2912 */
+int awkward_RegularArray_getitem_jagged_expand_64(int64_t* multistarts, int64_t* multistops, const int64_t* singleoffsets, int64_t regularsize, int64_t regularlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_RegularArray_getitem_next_range: replaces awkward-cpp/src/cpu-kernels/awkward_RegularArray_getitem_next_range.cpp:8 */
+/* kernel-specification.yml:3014 */
+int awkward_RegularArray_getitem_next_range_64(int64_t* tocarry, int64_t regular_start, int64_t step, int64_t length, int64_t size, int64_t nextsize, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_argmax: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_argmax.cpp:9 */
+/* kernel-specification.yml:4227 */
+int awkward_reduce_argmax_int8_64(int64_t* toptr, const int8_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4234 */
+int awkward_reduce_argmax_uint8_64(int64_t* toptr, const uint8_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4241 */
+int awkward_reduce_argmax_int16_64(int64_t* toptr, const int16_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4248 */
+int awkward_reduce_argmax_uint16_64(int64_t* toptr, const uint16_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4255 */
+int awkward_reduce_argmax_int32_64(int64_t* toptr, const int32_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4262 */
+int awkward_reduce_argmax_uint32_64(int64_t* toptr, const uint32_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4269 */
+int awkward_reduce_argmax_int64_64(int64_t* toptr, const int64_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4276 */
+int awkward_reduce_argmax_uint64_64(int64_t* toptr, const uint64_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4283 */
+int awkward_reduce_argmax_float32_64(int64_t* toptr, const float* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4290 */
+int awkward_reduce_argmax_float64_64(int64_t* toptr, const double* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_argmin: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_argmin.cpp:25 */
+/* kernel-specification.yml:4338 */
+int awkward_reduce_argmin_int8_64(int64_t* toptr, const int8_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4345 */
+int awkward_reduce_argmin_uint8_64(int64_t* toptr, const uint8_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4352 */
+int awkward_reduce_argmin_int16_64(int64_t* toptr, const int16_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4359 */
+int awkward_reduce_argmin_uint16_64(int64_t* toptr, const uint16_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4366 */
+int awkward_reduce_argmin_int32_64(int64_t* toptr, const int32_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4373 */
+int awkward_reduce_argmin_uint32_64(int64_t* toptr, const uint32_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4380 */
+int awkward_reduce_argmin_int64_64(int64_t* toptr, const int64_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4387 */
+int awkward_reduce_argmin_uint64_64(int64_t* toptr, const uint64_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4394 */
+int awkward_reduce_argmin_float32_64(int64_t* toptr, const float* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4401 */
+int awkward_reduce_argmin_float64_64(int64_t* toptr, const double* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_count_64: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_count_64.cpp:7 */
+/* kernel-specification.yml:4449 */
+int awkward_reduce_count_64(int64_t* toptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_countnonzero: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_countnonzero.cpp:14 */
+/* kernel-specification.yml:4462 */
+int awkward_reduce_countnonzero_bool_64(int64_t* toptr, const bool* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4468 */
+int awkward_reduce_countnonzero_int8_64(int64_t* toptr, const int8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4474 */
+int awkward_reduce_countnonzero_uint8_64(int64_t* toptr, const uint8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4480 */
+int awkward_reduce_countnonzero_int16_64(int64_t* toptr, const int16_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4486 */
+int awkward_reduce_countnonzero_uint16_64(int64_t* toptr, const uint16_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4492 */
+int awkward_reduce_countnonzero_int32_64(int64_t* toptr, const int32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4498 */
+int awkward_reduce_countnonzero_uint32_64(int64_t* toptr, const uint32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4504 */
+int awkward_reduce_countnonzero_int64_64(int64_t* toptr, const int64_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4510 */
+int awkward_reduce_countnonzero_uint64_64(int64_t* toptr, const uint64_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4516 */
+int awkward_reduce_countnonzero_float32_64(int64_t* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4522 */
+int awkward_reduce_countnonzero_float64_64(int64_t* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_max: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_max.cpp:9 */
+/* kernel-specification.yml:4564 */
+int awkward_reduce_max_int8_int8_64(int8_t* toptr, const int8_t* fromptr, const int64_t* offsets, int64_t outlength, int8_t identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4571 */
+int awkward_reduce_max_uint8_uint8_64(uint8_t* toptr, const uint8_t* fromptr, const int64_t* offsets, int64_t outlength, uint8_t identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4578 */
+int awkward_reduce_max_int16_int16_64(int16_t* toptr, const int16_t* fromptr, const int64_t* offsets, int64_t outlength, int16_t identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4585 */
+int awkward_reduce_max_uint16_uint16_64(uint16_t* toptr, const uint16_t* fromptr, const int64_t* offsets, int64_t outlength, uint16_t identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4592 */
+int awkward_reduce_max_int32_int32_64(int32_t* toptr, const int32_t* fromptr, const int64_t* offsets, int64_t outlength, int32_t identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4599 */
+int awkward_reduce_max_uint32_uint32_64(uint32_t* toptr, const uint32_t* fromptr, const int64_t* offsets, int64_t outlength, uint32_t identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4606 */
+int awkward_reduce_max_int64_int64_64(int64_t* toptr, const int64_t* fromptr, const int64_t* offsets, int64_t outlength, int64_t identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4613 */
+int awkward_reduce_max_uint64_uint64_64(uint64_t* toptr, const uint64_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4620 */
+int awkward_reduce_max_float32_float32_64(float* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, float identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4627 */
+int awkward_reduce_max_float64_float64_64(double* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, double identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_min: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_min.cpp:26 */
+/* kernel-specification.yml:4680 */
+int awkward_reduce_min_int8_int8_64(int8_t* toptr, const int8_t* fromptr, const int64_t* offsets, int64_t outlength, int8_t identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4687 */
+int awkward_reduce_min_uint8_uint8_64(uint8_t* toptr, const uint8_t* fromptr, const int64_t* offsets, int64_t outlength, uint8_t identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4694 */
+int awkward_reduce_min_int16_int16_64(int16_t* toptr, const int16_t* fromptr, const int64_t* offsets, int64_t outlength, int16_t identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4701 */
+int awkward_reduce_min_uint16_uint16_64(uint16_t* toptr, const uint16_t* fromptr, const int64_t* offsets, int64_t outlength, uint16_t identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4708 */
+int awkward_reduce_min_int32_int32_64(int32_t* toptr, const int32_t* fromptr, const int64_t* offsets, int64_t outlength, int32_t identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4715 */
+int awkward_reduce_min_uint32_uint32_64(uint32_t* toptr, const uint32_t* fromptr, const int64_t* offsets, int64_t outlength, uint32_t identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4722 */
+int awkward_reduce_min_int64_int64_64(int64_t* toptr, const int64_t* fromptr, const int64_t* offsets, int64_t outlength, int64_t identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4729 */
+int awkward_reduce_min_uint64_uint64_64(uint64_t* toptr, const uint64_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4736 */
+int awkward_reduce_min_float32_float32_64(float* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, float identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4743 */
+int awkward_reduce_min_float64_float64_64(double* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, double identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_prod: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_prod.cpp:12 */
+/* kernel-specification.yml:4796 */
+int awkward_reduce_prod_int64_int8_64(int64_t* toptr, const int8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4802 */
+int awkward_reduce_prod_uint64_uint8_64(uint64_t* toptr, const uint8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4808 */
+int awkward_reduce_prod_int64_int16_64(int64_t* toptr, const int16_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4814 */
+int awkward_reduce_prod_uint64_uint16_64(uint64_t* toptr, const uint16_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4820 */
+int awkward_reduce_prod_int64_int32_64(int64_t* toptr, const int32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4826 */
+int awkward_reduce_prod_uint64_uint32_64(uint64_t* toptr, const uint32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4832 */
+int awkward_reduce_prod_int64_int64_64(int64_t* toptr, const int64_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4838 */
+int awkward_reduce_prod_uint64_uint64_64(uint64_t* toptr, const uint64_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4844 */
+int awkward_reduce_prod_float32_float32_64(float* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4850 */
+int awkward_reduce_prod_float64_float64_64(double* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4856 */
+int awkward_reduce_prod_int32_int8_64(int32_t* toptr, const int8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4862 */
+int awkward_reduce_prod_uint32_uint8_64(uint32_t* toptr, const uint8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4868 */
+int awkward_reduce_prod_int32_int16_64(int32_t* toptr, const int16_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4874 */
+int awkward_reduce_prod_uint32_uint16_64(uint32_t* toptr, const uint16_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4880 */
+int awkward_reduce_prod_int32_int32_64(int32_t* toptr, const int32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4886 */
+int awkward_reduce_prod_uint32_uint32_64(uint32_t* toptr, const uint32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_prod_bool: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_prod_bool.cpp:10 */
+/* kernel-specification.yml:4933 */
+int awkward_reduce_prod_bool_bool_64(bool* toptr, const bool* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4939 */
+int awkward_reduce_prod_bool_int8_64(bool* toptr, const int8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4945 */
+int awkward_reduce_prod_bool_uint8_64(bool* toptr, const uint8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4951 */
+int awkward_reduce_prod_bool_int16_64(bool* toptr, const int16_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4957 */
+int awkward_reduce_prod_bool_uint16_64(bool* toptr, const uint16_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4963 */
+int awkward_reduce_prod_bool_int32_64(bool* toptr, const int32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4969 */
+int awkward_reduce_prod_bool_uint32_64(bool* toptr, const uint32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4975 */
+int awkward_reduce_prod_bool_int64_64(bool* toptr, const int64_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4981 */
+int awkward_reduce_prod_bool_uint64_64(bool* toptr, const uint64_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4987 */
+int awkward_reduce_prod_bool_float32_64(bool* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4993 */
+int awkward_reduce_prod_bool_float64_64(bool* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_sum: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_sum.cpp:12 */
+/* kernel-specification.yml:5037 */
+int awkward_reduce_sum_int64_int8_64(int64_t* toptr, const int8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5043 */
+int awkward_reduce_sum_uint64_uint8_64(uint64_t* toptr, const uint8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5049 */
+int awkward_reduce_sum_int64_int16_64(int64_t* toptr, const int16_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5055 */
+int awkward_reduce_sum_uint64_uint16_64(uint64_t* toptr, const uint16_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5061 */
+int awkward_reduce_sum_int64_int32_64(int64_t* toptr, const int32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5067 */
+int awkward_reduce_sum_uint64_uint32_64(uint64_t* toptr, const uint32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5073 */
+int awkward_reduce_sum_int64_int64_64(int64_t* toptr, const int64_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5079 */
+int awkward_reduce_sum_uint64_uint64_64(uint64_t* toptr, const uint64_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5085 */
+int awkward_reduce_sum_float32_float32_64(float* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5091 */
+int awkward_reduce_sum_float64_float64_64(double* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5097 */
+int awkward_reduce_sum_int32_int8_64(int32_t* toptr, const int8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5103 */
+int awkward_reduce_sum_uint32_uint8_64(uint32_t* toptr, const uint8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5109 */
+int awkward_reduce_sum_int32_int16_64(int32_t* toptr, const int16_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5115 */
+int awkward_reduce_sum_uint32_uint16_64(uint32_t* toptr, const uint16_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5121 */
+int awkward_reduce_sum_int32_int32_64(int32_t* toptr, const int32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5127 */
+int awkward_reduce_sum_uint32_uint32_64(uint32_t* toptr, const uint32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5133 */
+int awkward_reduce_sum_float64_int8_64(double* toptr, const int8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5139 */
+int awkward_reduce_sum_float64_uint8_64(double* toptr, const uint8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5145 */
+int awkward_reduce_sum_float64_int16_64(double* toptr, const int16_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5151 */
+int awkward_reduce_sum_float64_uint16_64(double* toptr, const uint16_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5157 */
+int awkward_reduce_sum_float64_int32_64(double* toptr, const int32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5163 */
+int awkward_reduce_sum_float64_uint32_64(double* toptr, const uint32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5169 */
+int awkward_reduce_sum_float64_int64_64(double* toptr, const int64_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5175 */
+int awkward_reduce_sum_float64_uint64_64(double* toptr, const uint64_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5181 */
+int awkward_reduce_sum_float64_float32_64(double* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_sumofsquares: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_sumofsquares.cpp:12 */
+/* kernel-specification.yml:5198 */
+int awkward_reduce_sumofsquares_float64_int8_64(double* toptr, const int8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5204 */
+int awkward_reduce_sumofsquares_float64_uint8_64(double* toptr, const uint8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5210 */
+int awkward_reduce_sumofsquares_float64_int16_64(double* toptr, const int16_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5216 */
+int awkward_reduce_sumofsquares_float64_uint16_64(double* toptr, const uint16_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5222 */
+int awkward_reduce_sumofsquares_float64_int32_64(double* toptr, const int32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5228 */
+int awkward_reduce_sumofsquares_float64_uint32_64(double* toptr, const uint32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5234 */
+int awkward_reduce_sumofsquares_float64_int64_64(double* toptr, const int64_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5240 */
+int awkward_reduce_sumofsquares_float64_uint64_64(double* toptr, const uint64_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5246 */
+int awkward_reduce_sumofsquares_float64_bool_64(double* toptr, const bool* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5252 */
+int awkward_reduce_sumofsquares_float64_float32_64(double* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5258 */
+int awkward_reduce_sumofsquares_float64_float64_64(double* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_sumofpowers: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_sumofpowers.cpp:39 */
+/* kernel-specification.yml:5275 */
+int awkward_reduce_sumofpowers_float64_int8_64(double* toptr, const int8_t* fromptr, const int64_t* offsets, int64_t outlength, int64_t n, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5282 */
+int awkward_reduce_sumofpowers_float64_uint8_64(double* toptr, const uint8_t* fromptr, const int64_t* offsets, int64_t outlength, int64_t n, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5289 */
+int awkward_reduce_sumofpowers_float64_int16_64(double* toptr, const int16_t* fromptr, const int64_t* offsets, int64_t outlength, int64_t n, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5296 */
+int awkward_reduce_sumofpowers_float64_uint16_64(double* toptr, const uint16_t* fromptr, const int64_t* offsets, int64_t outlength, int64_t n, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5303 */
+int awkward_reduce_sumofpowers_float64_int32_64(double* toptr, const int32_t* fromptr, const int64_t* offsets, int64_t outlength, int64_t n, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5310 */
+int awkward_reduce_sumofpowers_float64_uint32_64(double* toptr, const uint32_t* fromptr, const int64_t* offsets, int64_t outlength, int64_t n, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5317 */
+int awkward_reduce_sumofpowers_float64_int64_64(double* toptr, const int64_t* fromptr, const int64_t* offsets, int64_t outlength, int64_t n, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5324 */
+int awkward_reduce_sumofpowers_float64_uint64_64(double* toptr, const uint64_t* fromptr, const int64_t* offsets, int64_t outlength, int64_t n, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5331 */
+int awkward_reduce_sumofpowers_float64_bool_64(double* toptr, const bool* fromptr, const int64_t* offsets, int64_t outlength, int64_t n, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5338 */
+int awkward_reduce_sumofpowers_float64_float32_64(double* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, int64_t n, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5345 */
+int awkward_reduce_sumofpowers_float64_float64_64(double* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, int64_t n, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_centered_sumofsquares: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_centered_sumofsquares.cpp:15 */
+/* kernel-specification.yml:5363 */
+int awkward_reduce_centered_sumofsquares_float64_int8_64(double* toptr, const int8_t* fromptr, const int64_t* offsets, int64_t outlength, const double* means, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5370 */
+int awkward_reduce_centered_sumofsquares_float64_uint8_64(double* toptr, const uint8_t* fromptr, const int64_t* offsets, int64_t outlength, const double* means, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5377 */
+int awkward_reduce_centered_sumofsquares_float64_int16_64(double* toptr, const int16_t* fromptr, const int64_t* offsets, int64_t outlength, const double* means, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5384 */
+int awkward_reduce_centered_sumofsquares_float64_uint16_64(double* toptr, const uint16_t* fromptr, const int64_t* offsets, int64_t outlength, const double* means, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5391 */
+int awkward_reduce_centered_sumofsquares_float64_int32_64(double* toptr, const int32_t* fromptr, const int64_t* offsets, int64_t outlength, const double* means, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5398 */
+int awkward_reduce_centered_sumofsquares_float64_uint32_64(double* toptr, const uint32_t* fromptr, const int64_t* offsets, int64_t outlength, const double* means, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5405 */
+int awkward_reduce_centered_sumofsquares_float64_int64_64(double* toptr, const int64_t* fromptr, const int64_t* offsets, int64_t outlength, const double* means, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5412 */
+int awkward_reduce_centered_sumofsquares_float64_uint64_64(double* toptr, const uint64_t* fromptr, const int64_t* offsets, int64_t outlength, const double* means, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5419 */
+int awkward_reduce_centered_sumofsquares_float64_bool_64(double* toptr, const bool* fromptr, const int64_t* offsets, int64_t outlength, const double* means, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5426 */
+int awkward_reduce_centered_sumofsquares_float64_float32_64(double* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, const double* means, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5433 */
+int awkward_reduce_centered_sumofsquares_float64_float64_64(double* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, const double* means, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_sum_bool: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_sum_bool.cpp:18 */
+/* kernel-specification.yml:5479 */
+int awkward_reduce_sum_bool_bool_64(bool* toptr, const bool* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5485 */
+int awkward_reduce_sum_bool_int8_64(bool* toptr, const int8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5491 */
+int awkward_reduce_sum_bool_uint8_64(bool* toptr, const uint8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5497 */
+int awkward_reduce_sum_bool_int16_64(bool* toptr, const int16_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5503 */
+int awkward_reduce_sum_bool_uint16_64(bool* toptr, const uint16_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5509 */
+int awkward_reduce_sum_bool_int32_64(bool* toptr, const int32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5515 */
+int awkward_reduce_sum_bool_uint32_64(bool* toptr, const uint32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5521 */
+int awkward_reduce_sum_bool_int64_64(bool* toptr, const int64_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5527 */
+int awkward_reduce_sum_bool_uint64_64(bool* toptr, const uint64_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5533 */
+int awkward_reduce_sum_bool_float32_64(bool* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5539 */
+int awkward_reduce_sum_bool_float64_64(bool* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_sum_int32_bool_64: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_sum_int32_bool_64.cpp:7 */
+/* kernel-specification.yml:5583 */
+int awkward_reduce_sum_int32_bool_64(int32_t* toptr, const bool* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_sum_int64_bool_64: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_sum_int64_bool_64.cpp:7 */
+/* kernel-specification.yml:5601 */
+int awkward_reduce_sum_int64_bool_64(int64_t* toptr, const bool* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AWKWARD_GB300_H_ */

@@ -1,0 +1,688 @@
+/* awkward_oracle.c -- CPU oracle for the GB300 jagged hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file restates, in plain C, the awkward-cpp
+ * CPU kernels that libawkward_gb300 replaces, so that the CUDA results can be
+ * checked against the reference algorithm on the same inputs.  Only the test
+ * suite, the smoke check and the CPU-baseline leg of bench.py load it; the
+ * product path never calls it.
+ *
+ * Every function has the exact name and C signature of the awkward-cpp
+ * specialization it restates (kernel-specification.yml) and returns the same
+ * `struct Error` (awkward-cpp/include/awkward/common.h:39-77): str == NULL on
+ * success, else the message, the failing outer index (identity) and the
+ * offending value (attempt, kSliceNone when none).
+ *
+ * Parity is pinned two ways (tests/test_oracle_golden.py):
+ *   - awkward's kernel-test-data.json unit tests for every family here that
+ *     has them (fixtures in tests/golden/kernel_test_data_subset.json);
+ *   - outputs of awkward-cpp's own CPU kernels, compiled from the reference
+ *     sources by oracle/build.py, on seeded random inputs
+ *     (tests/golden/ref_random_*.npz).
+ *
+ * A pthread driver at the end (oracle_parallel_reduce) splits a reduction
+ * over list ranges for the multi-core CPU baseline.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdbool.h>
+#include <stddef.h>
+#include <stdint.h>
+#include <stdlib.h>
+
+struct Error {
+  const char* str;
+  const char* filename;
+  int64_t identity;
+  int64_t attempt;
+};
+
+#define kSliceNone ((int64_t)9223372036854775807LL)
+
+static struct Error success(void) {
+  struct Error e = {NULL, NULL, kSliceNone, kSliceNone};
+  return e;
+}
+static struct Error failure(const char* s, int64_t identity, int64_t attempt) {
+  struct Error e = {s, "oracle/awkward_oracle.c", identity, attempt};
+  return e;
+}
+
+/* ======================================================================
+ * Segmented reducers over offsets (awkward-cpp/src/cpu-kernels/awkward_reduce_*.cpp)
+ * Every reducer visits bin b's elements fromptr[offsets[b] .. offsets[b+1])
+ * in order, left to right, accumulating in the output type.
+ * ====================================================================== */
+
+/* awkward_reduce_sum.cpp:12-25 -- acc = OUT{}; acc += (OUT)x */
+#define ORACLE_SUM(NAME, OUT, IN)                                              \
+  struct Error NAME(OUT* toptr, const IN* fromptr, const int64_t* offsets,     \
+                    int64_t outlength) {                                       \
+    for (int64_t b = 0; b < outlength; b++) {                                  \
+      OUT acc = (OUT)0;                                                        \
+      for (int64_t i = offsets[b]; i < offsets[b + 1]; i++) acc += (OUT)fromptr[i]; \
+      toptr[b] = acc;                                                          \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_SUM(awkward_reduce_sum_int64_int8_64, int64_t, int8_t)
+ORACLE_SUM(awkward_reduce_sum_uint64_uint8_64, uint64_t, uint8_t)
+ORACLE_SUM(awkward_reduce_sum_int64_int16_64, int64_t, int16_t)
+ORACLE_SUM(awkward_reduce_sum_uint64_uint16_64, uint64_t, uint16_t)
+ORACLE_SUM(awkward_reduce_sum_int64_int32_64, int64_t, int32_t)
+ORACLE_SUM(awkward_reduce_sum_uint64_uint32_64, uint64_t, uint32_t)
+ORACLE_SUM(awkward_reduce_sum_int64_int64_64, int64_t, int64_t)
+ORACLE_SUM(awkward_reduce_sum_uint64_uint64_64, uint64_t, uint64_t)
+ORACLE_SUM(awkward_reduce_sum_float32_float32_64, float, float)
+ORACLE_SUM(awkward_reduce_sum_float64_float64_64, double, double)
+ORACLE_SUM(awkward_reduce_sum_int32_int8_64, int32_t, int8_t)
+ORACLE_SUM(awkward_reduce_sum_uint32_uint8_64, uint32_t, uint8_t)
+ORACLE_SUM(awkward_reduce_sum_int32_int16_64, int32_t, int16_t)
+ORACLE_SUM(awkward_reduce_sum_uint32_uint16_64, uint32_t, uint16_t)
+ORACLE_SUM(awkward_reduce_sum_int32_int32_64, int32_t, int32_t)
+ORACLE_SUM(awkward_reduce_sum_uint32_uint32_64, uint32_t, uint32_t)
+ORACLE_SUM(awkward_reduce_sum_float64_int8_64, double, int8_t)
+ORACLE_SUM(awkward_reduce_sum_float64_uint8_64, double, uint8_t)
+ORACLE_SUM(awkward_reduce_sum_float64_int16_64, double, int16_t)
+ORACLE_SUM(awkward_reduce_sum_float64_uint16_64, double, uint16_t)
+ORACLE_SUM(awkward_reduce_sum_float64_int32_64, double, int32_t)
+ORACLE_SUM(awkward_reduce_sum_float64_uint32_64, double, uint32_t)
+ORACLE_SUM(awkward_reduce_sum_float64_int64_64, double, int64_t)
+ORACLE_SUM(awkward_reduce_sum_float64_uint64_64, double, uint64_t)
+ORACLE_SUM(awkward_reduce_sum_float64_float32_64, double, float)
+
+/* awkward_reduce_sum_int32_bool_64.cpp:7-19, awkward_reduce_sum_int64_bool_64.cpp:7-19 */
+#define ORACLE_SUM_OF_BOOL(NAME, OUT)                                          \
+  struct Error NAME(OUT* toptr, const bool* fromptr, const int64_t* offsets,   \
+                    int64_t outlength) {                                       \
+    for (int64_t b = 0; b < outlength; b++) {                                  \
+      OUT acc = 0;                                                             \
+      for (int64_t i = offsets[b]; i < offsets[b + 1]; i++) if (fromptr[i]) acc++; \
+      toptr[b] = acc;                                                          \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_SUM_OF_BOOL(awkward_reduce_sum_int32_bool_64, int32_t)
+ORACLE_SUM_OF_BOOL(awkward_reduce_sum_int64_bool_64, int64_t)
+
+/* awkward_reduce_sum_bool.cpp:18-31 (any nonzero) and
+ * awkward_reduce_prod_bool.cpp:10-23 (all nonzero); NaN != 0 is true. */
+#define ORACLE_ANY(NAME, IN)                                                   \
+  struct Error NAME(bool* toptr, const IN* fromptr, const int64_t* offsets,    \
+                    int64_t outlength) {                                       \
+    for (int64_t b = 0; b < outlength; b++) {                                  \
+      bool found = false;                                                      \
+      for (int64_t i = offsets[b]; i < offsets[b + 1]; i++)                    \
+        if (fromptr[i] != 0) { found = true; break; }                          \
+      toptr[b] = found;                                                        \
+    }                                                                          \
+    return success();                                                          \
+  }
+#define ORACLE_ALL(NAME, IN)                                                   \
+  struct Error NAME(bool* toptr, const IN* fromptr, const int64_t* offsets,    \
+                    int64_t outlength) {                                       \
+    for (int64_t b = 0; b < outlength; b++) {                                  \
+      bool all = true;                                                         \
+      for (int64_t i = offsets[b]; i < offsets[b + 1]; i++)                    \
+        if (fromptr[i] == 0) { all = false; break; }                           \
+      toptr[b] = all;                                                          \
+    }                                                                          \
+    return success();                                                          \
+  }
+#define ORACLE_FOR_ALL_IN(M, PREFIX)                                           \
+  M(PREFIX##bool_64, bool) M(PREFIX##int8_64, int8_t) M(PREFIX##uint8_64, uint8_t) \
+  M(PREFIX##int16_64, int16_t) M(PREFIX##uint16_64, uint16_t)                  \
+  M(PREFIX##int32_64, int32_t) M(PREFIX##uint32_64, uint32_t)                  \
+  M(PREFIX##int64_64, int64_t) M(PREFIX##uint64_64, uint64_t)                  \
+  M(PREFIX##float32_64, float) M(PREFIX##float64_64, double)
+ORACLE_FOR_ALL_IN(ORACLE_ANY, awkward_reduce_sum_bool_)
+ORACLE_FOR_ALL_IN(ORACLE_ALL, awkward_reduce_prod_bool_)
+
+/* awkward_reduce_prod.cpp:12-25 -- acc = (OUT)1; acc *= (OUT)x */
+#define ORACLE_PROD(NAME, OUT, IN)                                             \
+  struct Error NAME(OUT* toptr, const IN* fromptr, const int64_t* offsets,     \
+                    int64_t outlength) {                                       \
+    for (int64_t b = 0; b < outlength; b++) {                                  \
+      OUT acc = (OUT)1;                                                        \
+      for (int64_t i = offsets[b]; i < offsets[b + 1]; i++) acc *= (OUT)fromptr[i]; \
+      toptr[b] = acc;                                                          \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_PROD(awkward_reduce_prod_int64_int8_64, int64_t, int8_t)
+ORACLE_PROD(awkward_reduce_prod_uint64_uint8_64, uint64_t, uint8_t)
+ORACLE_PROD(awkward_reduce_prod_int64_int16_64, int64_t, int16_t)
+ORACLE_PROD(awkward_reduce_prod_uint64_uint16_64, uint64_t, uint16_t)
+ORACLE_PROD(awkward_reduce_prod_int64_int32_64, int64_t, int32_t)
+ORACLE_PROD(awkward_reduce_prod_uint64_uint32_64, uint64_t, uint32_t)
+ORACLE_PROD(awkward_reduce_prod_int64_int64_64, int64_t, int64_t)
+ORACLE_PROD(awkward_reduce_prod_uint64_uint64_64, uint64_t, uint64_t)
+ORACLE_PROD(awkward_reduce_prod_float32_float32_64, float, float)
+ORACLE_PROD(awkward_reduce_prod_float64_float64_64, double, double)
+ORACLE_PROD(awkward_reduce_prod_int32_int8_64, int32_t, int8_t)
+ORACLE_PROD(awkward_reduce_prod_uint32_uint8_64, uint32_t, uint8_t)
+ORACLE_PROD(awkward_reduce_prod_int32_int16_64, int32_t, int16_t)
+ORACLE_PROD(awkward_reduce_prod_uint32_uint16_64, uint32_t, uint16_t)
+ORACLE_PROD(awkward_reduce_prod_int32_int32_64, int32_t, int32_t)
+ORACLE_PROD(awkward_reduce_prod_uint32_uint32_64, uint32_t, uint32_t)
+
+/* awkward_reduce_max.cpp:9-26 / awkward_reduce_min.cpp:26-43 --
+ * best = identity; best = (v > best) ? v : best.  NaN never replaces best;
+ * among equal values (e.g. -0.0 and +0.0) the earliest, identity first, stays. */
+#define ORACLE_EXTREMUM(NAME, T, CMP)                                          \
+  struct Error NAME(T* toptr, const T* fromptr, const int64_t* offsets,        \
+                    int64_t outlength, T identity) {                           \
+    for (int64_t b = 0; b < outlength; b++) {                                  \
+      T best = identity;                                                       \
+      for (int64_t i = offsets[b]; i < offsets[b + 1]; i++) {                  \
+        T v = fromptr[i];                                                      \
+        best = (v CMP best) ? v : best;                                        \
+      }                                                                        \
+      toptr[b] = best;                                                         \
+    }                                                                          \
+    return success();                                                          \
+  }
+#define ORACLE_FOR_NUMERIC_SAME(M, PREFIX, CMP)                                \
+  M(PREFIX##int8_int8_64, int8_t, CMP) M(PREFIX##uint8_uint8_64, uint8_t, CMP) \
+  M(PREFIX##int16_int16_64, int16_t, CMP) M(PREFIX##uint16_uint16_64, uint16_t, CMP) \
+  M(PREFIX##int32_int32_64, int32_t, CMP) M(PREFIX##uint32_uint32_64, uint32_t, CMP) \
+  M(PREFIX##int64_int64_64, int64_t, CMP) M(PREFIX##uint64_uint64_64, uint64_t, CMP) \
+  M(PREFIX##float32_float32_64, float, CMP) M(PREFIX##float64_float64_64, double, CMP)
+ORACLE_FOR_NUMERIC_SAME(ORACLE_EXTREMUM, awkward_reduce_max_, >)
+ORACLE_FOR_NUMERIC_SAME(ORACLE_EXTREMUM, awkward_reduce_min_, <)
+
+/* awkward_reduce_argmax.cpp:9-33 / awkward_reduce_argmin.cpp:25-49 --
+ * global index of the first extremum; -1 for an empty bin.  The first
+ * element is taken unconditionally, so a leading NaN wins; later NaNs never
+ * win.  `starts` is unused. */
+#define ORACLE_ARG(NAME, IN, CMP)                                              \
+  struct Error NAME(int64_t* toptr, const IN* fromptr, const int64_t* offsets, \
+                    const int64_t* starts, int64_t outlength) {                \
+    (void)starts;                                                              \
+    for (int64_t b = 0; b < outlength; b++) {                                  \
+      int64_t start = offsets[b], stop = offsets[b + 1], best = -1;            \
+      if (start < stop) {                                                      \
+        best = start;                                                          \
+        IN bv = fromptr[start];                                                \
+        for (int64_t i = start + 1; i < stop; i++)                             \
+          if (fromptr[i] CMP bv) { bv = fromptr[i]; best = i; }                \
+      }                                                                        \
+      toptr[b] = best;                                                         \
+    }                                                                          \
+    return success();                                                          \
+  }
+#define ORACLE_FOR_NUMERIC_IN(M, PREFIX, CMP)                                  \
+  M(PREFIX##int8_64, int8_t, CMP) M(PREFIX##uint8_64, uint8_t, CMP)            \
+  M(PREFIX##int16_64, int16_t, CMP) M(PREFIX##uint16_64, uint16_t, CMP)        \
+  M(PREFIX##int32_64, int32_t, CMP) M(PREFIX##uint32_64, uint32_t, CMP)        \
+  M(PREFIX##int64_64, int64_t, CMP) M(PREFIX##uint64_64, uint64_t, CMP)        \
+  M(PREFIX##float32_64, float, CMP) M(PREFIX##float64_64, double, CMP)
+ORACLE_FOR_NUMERIC_IN(ORACLE_ARG, awkward_reduce_argmax_, >)
+ORACLE_FOR_NUMERIC_IN(ORACLE_ARG, awkward_reduce_argmin_, <)
+
+/* awkward_reduce_count_64.cpp:7-15 */
+struct Error awkward_reduce_count_64(int64_t* toptr, const int64_t* offsets,
+                                     int64_t outlength) {
+  for (int64_t b = 0; b < outlength; b++) toptr[b] = offsets[b + 1] - offsets[b];
+  return success();
+}
+
+/* awkward_reduce_countnonzero.cpp:14-36 */
+#define ORACLE_COUNTNONZERO(NAME, IN)                                          \
+  struct Error NAME(int64_t* toptr, const IN* fromptr, const int64_t* offsets, \
+                    int64_t outlength) {                                       \
+    for (int64_t b = 0; b < outlength; b++) {                                  \
+      int64_t c = 0;                                                           \
+      for (int64_t i = offsets[b]; i < offsets[b + 1]; i++) c += (fromptr[i] != 0); \
+      toptr[b] = c;                                                            \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_FOR_ALL_IN(ORACLE_COUNTNONZERO, awkward_reduce_countnonzero_)
+
+/* awkward_reduce_sumofsquares.cpp:12-25: acc += v*v with v = (double)x */
+#define ORACLE_SUMSQ(NAME, IN)                                                 \
+  struct Error NAME(double* toptr, const IN* fromptr, const int64_t* offsets,  \
+                    int64_t outlength) {                                       \
+    for (int64_t b = 0; b < outlength; b++) {                                  \
+      double acc = 0.0;                                                        \
+      for (int64_t i = offsets[b]; i < offsets[b + 1]; i++) {                  \
+        double v = (double)fromptr[i];                                         \
+        acc += v * v;                                                          \
+      }                                                                        \
+      toptr[b] = acc;                                                          \
+    }                                                                          \
+    return success();                                                          \
+  }
+#define ORACLE_FOR_F64_OUT(M, PREFIX)                                          \
+  M(PREFIX##float64_int8_64, int8_t) M(PREFIX##float64_uint8_64, uint8_t)      \
+  M(PREFIX##float64_int16_64, int16_t) M(PREFIX##float64_uint16_64, uint16_t)  \
+  M(PREFIX##float64_int32_64, int32_t) M(PREFIX##float64_uint32_64, uint32_t)  \
+  M(PREFIX##float64_int64_64, int64_t) M(PREFIX##float64_uint64_64, uint64_t)  \
+  M(PREFIX##float64_bool_64, bool) M(PREFIX##float64_float32_64, float)        \
+  M(PREFIX##float64_float64_64, double)
+ORACLE_FOR_F64_OUT(ORACLE_SUMSQ, awkward_reduce_sumofsquares_)
+
+/* awkward_reduce_sumofpowers.cpp:14-60: integer powers by repeated
+ * squaring (exponent bits low to high), std::pow for n < 0. */
+static double oracle_ipow(double base, int64_t n) {
+  if (n < 0) return pow(base, (double)n);
+  double result = 1.0, b = base;
+  int64_t e = n;
+  while (e > 0) {
+    if (e & 1) result *= b;
+    e >>= 1;
+    if (e > 0) b *= b;
+  }
+  return result;
+}
+#define ORACLE_SUMPOW(NAME, IN)                                                \
+  struct Error NAME(double* toptr, const IN* fromptr, const int64_t* offsets,  \
+                    int64_t outlength, int64_t n) {                            \
+    for (int64_t b = 0; b < outlength; b++) {                                  \
+      double acc = 0.0;                                                        \
+      for (int64_t i = offsets[b]; i < offsets[b + 1]; i++)                    \
+        acc += oracle_ipow((double)fromptr[i], n);                             \
+      toptr[b] = acc;                                                          \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_FOR_F64_OUT(ORACLE_SUMPOW, awkward_reduce_sumofpowers_)
+
+/* awkward_reduce_centered_sumofsquares.cpp:15-29: d = (double)x - means[b] */
+#define ORACLE_CSUMSQ(NAME, IN)                                                \
+  struct Error NAME(double* toptr, const IN* fromptr, const int64_t* offsets,  \
+                    int64_t outlength, const double* means) {                  \
+    for (int64_t b = 0; b < outlength; b++) {                                  \
+      double acc = 0.0, m = means[b];                                          \
+      for (int64_t i = offsets[b]; i < offsets[b + 1]; i++) {                  \
+        double d = (double)fromptr[i] - m;                                     \
+        acc += d * d;                                                          \
+      }                                                                        \
+      toptr[b] = acc;                                                          \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_FOR_F64_OUT(ORACLE_CSUMSQ, awkward_reduce_centered_sumofsquares_)
+
+/* awkward_NumpyArray_reduce_adjust_starts_64.cpp:7-25 */
+struct Error awkward_NumpyArray_reduce_adjust_starts_64(int64_t* toptr, int64_t outlength,
+                                                        const int64_t* offsets,
+                                                        const int64_t* starts) {
+  (void)offsets;
+  for (int64_t k = 0; k < outlength; k++)
+    if (toptr[k] >= 0) toptr[k] -= starts[k];
+  return success();
+}
+
+/* awkward_NumpyArray_reduce_mask_ByteMaskedArray_64.cpp:7-20 */
+struct Error awkward_NumpyArray_reduce_mask_ByteMaskedArray_64(int8_t* toptr,
+                                                               const int64_t* offsets,
+                                                               int64_t outlength) {
+  for (int64_t i = 0; i < outlength; i++) toptr[i] = (offsets[i + 1] - offsets[i] > 0) ? 0 : 1;
+  return success();
+}
+
+/* ======================================================================
+ * Jagged getitem (awkward-cpp/src/cpu-kernels/awkward_ListArray_getitem_jagged_*.cpp)
+ * ====================================================================== */
+
+/* awkward_ListArray_getitem_jagged_apply.cpp:8-56 */
+#define ORACLE_JAGGED_APPLY(NAME, C)                                           \
+  struct Error NAME(int64_t* tooffsets, int64_t* tocarry, const int64_t* slicestarts, \
+                    const int64_t* slicestops, int64_t sliceouterlen,          \
+                    const int64_t* sliceindex, int64_t sliceinnerlen,          \
+                    const C* fromstarts, const C* fromstops, int64_t contentlen) { \
+    int64_t k = 0;                                                             \
+    for (int64_t i = 0; i < sliceouterlen; i++) {                              \
+      int64_t ss = slicestarts[i], se = slicestops[i];                         \
+      tooffsets[i] = k;                                                        \
+      if (ss == se) continue;                                                  \
+      if (se < ss) return failure("jagged slice's stops[i] < starts[i]", i, kSliceNone); \
+      if (se > sliceinnerlen)                                                  \
+        return failure("jagged slice's offsets extend beyond its content", i, se); \
+      int64_t start = (int64_t)fromstarts[i], stop = (int64_t)fromstops[i];    \
+      if (stop < start) return failure("stops[i] < starts[i]", i, kSliceNone); \
+      if (start != stop && stop > contentlen)                                  \
+        return failure("stops[i] > len(content)", i, kSliceNone);              \
+      int64_t count = stop - start;                                            \
+      for (int64_t j = ss; j < se; j++) {                                      \
+        int64_t index = sliceindex[j];                                         \
+        if (index < -count || index >= count)                                  \
+          return failure("index out of range", i, index);                      \
+        if (index < 0) index += count;                                         \
+        tocarry[k++] = start + index;                                          \
+      }                                                                        \
+    }                                                                          \
+    tooffsets[sliceouterlen] = k;                                              \
+    return success();                                                          \
+  }
+ORACLE_JAGGED_APPLY(awkward_ListArray32_getitem_jagged_apply_64, int32_t)
+ORACLE_JAGGED_APPLY(awkward_ListArrayU32_getitem_jagged_apply_64, uint32_t)
+ORACLE_JAGGED_APPLY(awkward_ListArray64_getitem_jagged_apply_64, int64_t)
+
+/* awkward_ListArray_getitem_jagged_carrylen.cpp:8-18 */
+struct Error awkward_ListArray_getitem_jagged_carrylen_64(int64_t* carrylen,
+                                                         const int64_t* slicestarts,
+                                                         const int64_t* slicestops,
+                                                         int64_t sliceouterlen) {
+  int64_t total = 0;
+  for (int64_t i = 0; i < sliceouterlen; i++) total += slicestops[i] - slicestarts[i];
+  *carrylen = total;
+  return success();
+}
+
+/* awkward_ListArray_getitem_jagged_descend.cpp:8-31 */
+#define ORACLE_JAGGED_DESCEND(NAME, C)                                         \
+  struct Error NAME(int64_t* tooffsets, const int64_t* slicestarts,            \
+                    const int64_t* slicestops, int64_t sliceouterlen,          \
+                    const C* fromstarts, const C* fromstops) {                 \
+    tooffsets[0] = sliceouterlen == 0 ? 0 : slicestarts[0];                    \
+    for (int64_t i = 0; i < sliceouterlen; i++) {                              \
+      int64_t slicecount = slicestops[i] - slicestarts[i];                     \
+      int64_t count = (int64_t)(fromstops[i] - fromstarts[i]);                 \
+      if (slicecount != count)                                                 \
+        return failure("jagged slice inner length differs from array inner length", i, kSliceNone); \
+      tooffsets[i + 1] = tooffsets[i] + count;                                 \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_JAGGED_DESCEND(awkward_ListArray32_getitem_jagged_descend_64, int32_t)
+ORACLE_JAGGED_DESCEND(awkward_ListArrayU32_getitem_jagged_descend_64, uint32_t)
+ORACLE_JAGGED_DESCEND(awkward_ListArray64_getitem_jagged_descend_64, int64_t)
+
+/* awkward_ListArray_getitem_jagged_expand.cpp:8-32 */
+#define ORACLE_JAGGED_EXPAND(NAME, C)                                          \
+  struct Error NAME(int64_t* multistarts, int64_t* multistops,                 \
+                    const int64_t* singleoffsets, int64_t* tocarry,            \
+                    const C* fromstarts, const C* fromstops, int64_t jaggedsize, \
+                    int64_t length) {                                          \
+    for (int64_t i = 0; i < length; i++) {                                     \
+      C start = fromstarts[i], stop = fromstops[i];                            \
+      if (stop < start) return failure("stops[i] < starts[i]", i, kSliceNone); \
+      if ((int64_t)(stop - start) != jaggedsize)                               \
+        return failure("cannot fit jagged slice into nested list", i, kSliceNone); \
+      for (int64_t j = 0; j < jaggedsize; j++) {                               \
+        multistarts[i * jaggedsize + j] = singleoffsets[j];                    \
+        multistops[i * jaggedsize + j] = singleoffsets[j + 1];                 \
+        tocarry[i * jaggedsize + j] = (int64_t)start + j;                      \
+      }                                                                        \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_JAGGED_EXPAND(awkward_ListArray32_getitem_jagged_expand_64, int32_t)
+ORACLE_JAGGED_EXPAND(awkward_ListArrayU32_getitem_jagged_expand_64, uint32_t)
+ORACLE_JAGGED_EXPAND(awkward_ListArray64_getitem_jagged_expand_64, int64_t)
+
+/* awkward_ListArray_getitem_jagged_numvalid.cpp:8-30 */
+struct Error awkward_ListArray_getitem_jagged_numvalid_64(int64_t* numvalid,
+                                                         const int64_t* slicestarts,
+                                                         const int64_t* slicestops,
+                                                         int64_t length,
+                                                         const int64_t* missing,
+                                                         int64_t missinglength) {
+  int64_t total = 0;
+  *numvalid = 0;
+  for (int64_t i = 0; i < length; i++) {
+    int64_t ss = slicestarts[i], se = slicestops[i];
+    if (ss == se) continue;
+    if (se < ss) return failure("jagged slice's stops[i] < starts[i]", i, kSliceNone);
+    if (se > missinglength)
+      return failure("jagged slice's offsets extend beyond its content", i, se);
+    for (int64_t j = ss; j < se; j++) total += missing[j] >= 0 ? 1 : 0;
+    *numvalid = total;
+  }
+  *numvalid = total;
+  return success();
+}
+
+/* awkward_ListArray_getitem_jagged_shrink.cpp:8-46 */
+struct Error awkward_ListArray_getitem_jagged_shrink_64(int64_t* tocarry, int64_t* tosmalloffsets,
+                                                       int64_t* tolargeoffsets,
+                                                       const int64_t* slicestarts,
+                                                       const int64_t* slicestops, int64_t length,
+                                                       const int64_t* missing) {
+  int64_t k = 0;
+  tosmalloffsets[0] = length == 0 ? 0 : slicestarts[0];
+  tolargeoffsets[0] = length == 0 ? 0 : slicestarts[0];
+  for (int64_t i = 0; i < length; i++) {
+    int64_t ss = slicestarts[i], se = slicestops[i];
+    if (ss != se) {
+      int64_t small = 0;
+      for (int64_t j = ss; j < se; j++)
+        if (missing[j] >= 0) { tocarry[k++] = j; small++; }
+      tosmalloffsets[i + 1] = tosmalloffsets[i] + small;
+    } else {
+      tosmalloffsets[i + 1] = tosmalloffsets[i];
+    }
+    tolargeoffsets[i + 1] = tolargeoffsets[i] + (se - ss);
+  }
+  return success();
+}
+
+/* awkward_RegularArray_getitem_jagged_expand.cpp:8-20 */
+struct Error awkward_RegularArray_getitem_jagged_expand_64(int64_t* multistarts, int64_t* multistops,
+                                                          const int64_t* singleoffsets,
+                                                          int64_t regularsize,
+                                                          int64_t regularlength) {
+  for (int64_t i = 0; i < regularlength; i++)
+    for (int64_t j = 0; j < regularsize; j++) {
+      multistarts[i * regularsize + j] = singleoffsets[j];
+      multistops[i * regularsize + j] = singleoffsets[j + 1];
+    }
+  return success();
+}
+
+/* awkward_ListArray_localindex.cpp:8-19 */
+#define ORACLE_LOCALINDEX(NAME, C)                                             \
+  struct Error NAME(int64_t* toindex, const C* offsets, int64_t length) {      \
+    for (int64_t i = 0; i < length; i++) {                                     \
+      int64_t start = (int64_t)offsets[i], stop = (int64_t)offsets[i + 1];     \
+      for (int64_t j = start; j < stop; j++) toindex[j] = j - start;           \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_LOCALINDEX(awkward_ListArray32_localindex_64, int32_t)
+ORACLE_LOCALINDEX(awkward_ListArrayU32_localindex_64, uint32_t)
+ORACLE_LOCALINDEX(awkward_ListArray64_localindex_64, int64_t)
+
+/* ======================================================================
+ * Range slices (awkward_ListArray_getitem_next_range*.cpp, kernel-utils.cpp)
+ * ====================================================================== */
+
+/* kernel-utils.cpp:7-39: clip a Python slice against one list's length */
+static void oracle_regularize_rangeslice(int64_t* start, int64_t* stop, bool posstep,
+                                         bool hasstart, bool hasstop, int64_t length) {
+  if (posstep) {
+    if (!hasstart) *start = 0;
+    else if (*start < 0) *start += length;
+    if (*start < 0) *start = 0;
+    if (*start > length) *start = length;
+    if (!hasstop) *stop = length;
+    else if (*stop < 0) *stop += length;
+    if (*stop < 0) *stop = 0;
+    if (*stop > length) *stop = length;
+    if (*stop < *start) *stop = *start;
+  } else {
+    if (!hasstart) *start = length - 1;
+    else if (*start < 0) *start += length;
+    if (*start < -1) *start = -1;
+    if (*start > length - 1) *start = length - 1;
+    if (!hasstop) *stop = -1;
+    else if (*stop < 0) *stop += length;
+    if (*stop < -1) *stop = -1;
+    if (*stop > length - 1) *stop = length - 1;
+    if (*stop > *start) *stop = *start;
+  }
+}
+
+/* awkward_ListArray_getitem_next_range.cpp:9-41 */
+#define ORACLE_NEXT_RANGE(NAME, C)                                             \
+  struct Error NAME(C* tooffsets, int64_t* tocarry, const C* fromstarts,       \
+                    const C* fromstops, int64_t lenstarts, int64_t start,      \
+                    int64_t stop, int64_t step) {                              \
+    int64_t k = 0;                                                             \
+    tooffsets[0] = 0;                                                          \
+    for (int64_t i = 0; i < lenstarts; i++) {                                  \
+      int64_t length = (int64_t)fromstops[i] - (int64_t)fromstarts[i];         \
+      int64_t rs = start, re = stop;                                           \
+      oracle_regularize_rangeslice(&rs, &re, step > 0, start != kSliceNone,    \
+                                   stop != kSliceNone, length);                \
+      if (step > 0) {                                                          \
+        for (int64_t j = rs; j < re; j += step) tocarry[k++] = (int64_t)fromstarts[i] + j; \
+      } else {                                                                 \
+        for (int64_t j = rs; j > re; j += step) tocarry[k++] = (int64_t)fromstarts[i] + j; \
+      }                                                                        \
+      tooffsets[i + 1] = (C)k;                                                 \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_NEXT_RANGE(awkward_ListArray32_getitem_next_range_64, int32_t)
+ORACLE_NEXT_RANGE(awkward_ListArrayU32_getitem_next_range_64, uint32_t)
+ORACLE_NEXT_RANGE(awkward_ListArray64_getitem_next_range_64, int64_t)
+
+/* awkward_ListArray_getitem_next_range_carrylength.cpp:9-35 */
+#define ORACLE_NEXT_RANGE_CARRYLENGTH(NAME, C)                                 \
+  struct Error NAME(int64_t* carrylength, const C* fromstarts, const C* fromstops, \
+                    int64_t lenstarts, int64_t start, int64_t stop, int64_t step) { \
+    int64_t total = 0;                                                         \
+    for (int64_t i = 0; i < lenstarts; i++) {                                  \
+      int64_t length = (int64_t)fromstops[i] - (int64_t)fromstarts[i];         \
+      int64_t rs = start, re = stop;                                           \
+      oracle_regularize_rangeslice(&rs, &re, step > 0, start != kSliceNone,    \
+                                   stop != kSliceNone, length);                \
+      if (step > 0) { for (int64_t j = rs; j < re; j += step) total++; }       \
+      else { for (int64_t j = rs; j > re; j += step) total++; }                \
+    }                                                                          \
+    *carrylength = total;                                                      \
+    return success();                                                          \
+  }
+ORACLE_NEXT_RANGE_CARRYLENGTH(awkward_ListArray32_getitem_next_range_carrylength, int32_t)
+ORACLE_NEXT_RANGE_CARRYLENGTH(awkward_ListArrayU32_getitem_next_range_carrylength, uint32_t)
+ORACLE_NEXT_RANGE_CARRYLENGTH(awkward_ListArray64_getitem_next_range_carrylength, int64_t)
+
+/* awkward_RegularArray_getitem_next_range.cpp:8-19 */
+struct Error awkward_RegularArray_getitem_next_range_64(int64_t* tocarry, int64_t regular_start,
+                                                       int64_t step, int64_t length,
+                                                       int64_t size, int64_t nextsize) {
+  for (int64_t i = 0; i < length; i++)
+    for (int64_t j = 0; j < nextsize; j++)
+      tocarry[i * nextsize + j] = i * size + regular_start + j * step;
+  return success();
+}
+
+/* ======================================================================
+ * Combinations (awkward_ListArray_combinations*.cpp, kernel-utils.cpp:41-98)
+ * ====================================================================== */
+
+/* awkward_ListArray_combinations_length.cpp:8-45: C(size, n) by the
+ * multiplicative loop (size += n-1 with replacement); no overflow check. */
+#define ORACLE_COMBINATIONS_LENGTH(NAME, C)                                    \
+  struct Error NAME(int64_t* totallen, int64_t* tooffsets, int64_t n,          \
+                    bool replacement, const C* starts, const C* stops,         \
+                    int64_t length) {                                          \
+    int64_t total = 0;                                                         \
+    tooffsets[0] = 0;                                                          \
+    for (int64_t i = 0; i < length; i++) {                                     \
+      int64_t size = (int64_t)(stops[i] - starts[i]);                          \
+      if (replacement) size += n - 1;                                          \
+      int64_t thisn = n, len;                                                  \
+      if (thisn > size) len = 0;                                               \
+      else if (thisn == size) len = 1;                                         \
+      else {                                                                   \
+        if (thisn * 2 > size) thisn = size - thisn;                            \
+        len = size;                                                            \
+        for (int64_t j = 2; j <= thisn; j++) { len *= (size - j + 1); len /= j; } \
+      }                                                                        \
+      total += len;                                                            \
+      tooffsets[i + 1] = tooffsets[i] + len;                                   \
+    }                                                                          \
+    *totallen = total;                                                         \
+    return success();                                                          \
+  }
+ORACLE_COMBINATIONS_LENGTH(awkward_ListArray32_combinations_length_64, int32_t)
+ORACLE_COMBINATIONS_LENGTH(awkward_ListArrayU32_combinations_length_64, uint32_t)
+ORACLE_COMBINATIONS_LENGTH(awkward_ListArray64_combinations_length_64, int64_t)
+
+/* kernel-utils.cpp:41-80: depth-first lexicographic enumeration of the
+ * n-tuples of one list; fromindex[0..n) is the running tuple. */
+static void oracle_combinations_step(int64_t** tocarry, int64_t* toindex, int64_t* fromindex,
+                                     int64_t j, int64_t stop, int64_t n, bool replacement) {
+  while (fromindex[j] < stop) {
+    for (int64_t k = j + 1; k < n; k++)
+      fromindex[k] = replacement ? fromindex[j] : fromindex[j] + (k - j);
+    if (j + 1 == n) {
+      for (int64_t k = 0; k < n; k++) tocarry[k][toindex[k]++] = fromindex[k];
+    } else {
+      oracle_combinations_step(tocarry, toindex, fromindex, j + 1, stop, n, replacement);
+    }
+    fromindex[j]++;
+  }
+}
+
+/* awkward_ListArray_combinations.cpp:9-33 */
+#define ORACLE_COMBINATIONS(NAME, C)                                           \
+  struct Error NAME(int64_t** tocarry, int64_t* toindex, int64_t* fromindex,   \
+                    int64_t n, bool replacement, const C* starts, const C* stops, \
+                    int64_t length) {                                          \
+    for (int64_t j = 0; j < n; j++) toindex[j] = 0;                            \
+    for (int64_t i = 0; i < length; i++) {                                     \
+      fromindex[0] = (int64_t)starts[i];                                       \
+      oracle_combinations_step(tocarry, toindex, fromindex, 0, (int64_t)stops[i], n, \
+                               replacement);                                   \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_COMBINATIONS(awkward_ListArray32_combinations_64, int32_t)
+ORACLE_COMBINATIONS(awkward_ListArrayU32_combinations_64, uint32_t)
+ORACLE_COMBINATIONS(awkward_ListArray64_combinations_64, int64_t)
+
+/* ======================================================================
+ * Multi-core driver for the CPU baseline: run one reducer (any of the
+ * (toptr, fromptr, offsets, outlength) family above, or argmax/argmin with
+ * `starts`) over `nthreads` contiguous list ranges.  Each thread calls the
+ * single-threaded restatement on its own range; ranges never share an output.
+ * ====================================================================== */
+typedef struct Error (*oracle_reduce4_fn)(void*, const void*, const int64_t*, int64_t);
+typedef struct Error (*oracle_reduce5_fn)(void*, const void*, const int64_t*, const int64_t*, int64_t);
+
+typedef struct {
+  void* fn;
+  int kind; /* 4 = (to, from, offsets, n); 5 = argmax form (to, from, offsets, starts, n) */
+  char* toptr;
+  const void* fromptr;
+  const int64_t* offsets;
+  int64_t lo, hi;
+  size_t outsize;
+} oracle_job;
+
+static void* oracle_job_run(void* p) {
+  oracle_job* j = (oracle_job*)p;
+  if (j->kind == 4)
+    ((oracle_reduce4_fn)j->fn)(j->toptr + j->lo * j->outsize, j->fromptr, j->offsets + j->lo,
+                               j->hi - j->lo);
+  else
+    ((oracle_reduce5_fn)j->fn)(j->toptr + j->lo * j->outsize, j->fromptr, j->offsets + j->lo,
+                               NULL, j->hi - j->lo);
+  return NULL;
+}
+
+int oracle_parallel_reduce(void* fn, int kind, void* toptr, size_t outsize, const void* fromptr,
+                           const int64_t* offsets, int64_t outlength, int nthreads) {
+  if (nthreads < 1) nthreads = 1;
+  if (nthreads > 256) nthreads = 256;
+  pthread_t th[256];
+  oracle_job jobs[256];
+  for (int t = 0; t < nthreads; t++) {
+    jobs[t].fn = fn;
+    jobs[t].kind = kind;
+    jobs[t].toptr = (char*)toptr;
+    jobs[t].fromptr = fromptr;
+    jobs[t].offsets = offsets;
+    jobs[t].lo = outlength * t / nthreads;
+    jobs[t].hi = outlength * (t + 1) / nthreads;
+    jobs[t].outsize = outsize;
+    if (pthread_create(&th[t], NULL, oracle_job_run, &jobs[t]) != 0) return -1;
+  }
+  for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);
+  return 0;
+}

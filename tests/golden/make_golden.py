@@ -1,0 +1,297 @@
+"""Regenerate the committed golden fixtures (run by hand, where awkward's sources are).
+
+    python tests/golden/make_golden.py [/path/to/awkward]
+
+Writes two files next to this script:
+
+* ``kernel_test_data_subset.json`` -- the unit tests of awkward's
+  ``kernel-test-data.json`` for every kernel family libawkward_gb300 exports
+  (inputs, expected outputs, error flag and message), unchanged.
+* ``ref_random.npz`` -- seeded random cases for every family (including the
+  three with no unit tests: sumofsquares, sumofpowers, centered_sumofsquares),
+  each run through awkward-cpp's OWN CPU kernels compiled by
+  ``oracle/build.py``; stores inputs, the outputs after the call and the
+  returned error.  A JSON manifest (key ``manifest``) lists the cases.
+
+Both pin the C restatement in ``oracle/`` and are the fixtures of the GPU
+parity tests.  Nothing here runs at test time.
+"""
+
+from __future__ import annotations
+
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from awkward_gb300._signatures import SIGNATURES  # noqa: E402
+from awkward_gb300.gen_signatures import FAMILIES  # noqa: E402
+
+import oracle  # noqa: E402
+from oracle import NP_DTYPES  # noqa: E402
+
+SLICE_NONE = np.iinfo(np.int64).max
+
+
+def extract_unit_tests(awkward_src):
+    with open(os.path.join(awkward_src, "kernel-test-data.json")) as f:
+        data = json.load(f)["unit-tests"]
+    out = {}
+    for rec in data:
+        if rec["name"] in FAMILIES:
+            out[rec["name"]] = {"status": rec["status"], "tests": rec["tests"]}
+    with open(os.path.join(HERE, "kernel_test_data_subset.json"), "w") as f:
+        json.dump(out, f, separators=(",", ":"))
+    return sum(len(v["tests"]) for v in out.values())
+
+
+# ---------------------------------------------------------------- random inputs
+def _lengths(rng, n, lam, p_empty=0.05, longs=(33, 257, 1025)):
+    L = rng.poisson(lam, n).astype(np.int64)
+    L[rng.random(n) < p_empty] = 0
+    for k, ln in enumerate(longs):
+        if n > 3 * (k + 1):
+            L[rng.integers(0, n)] = ln
+    return L
+
+
+def _offsets(L):
+    return np.concatenate([[0], np.cumsum(L)]).astype(np.int64)
+
+
+def _values(rng, base, n):
+    dt = NP_DTYPES[base]
+    if base == "bool":
+        return rng.random(n) < 0.5
+    if base in ("float", "double"):
+        x = rng.standard_normal(n).astype(dt)
+        # exercise the comparison rules: NaN, signed zeros, infinities, ties
+        k = max(n // 40, 1)
+        for special in (np.nan, 0.0, -0.0, np.inf, -np.inf, 1.0):
+            idx = rng.integers(0, n, k) if n else np.zeros(0, np.int64)
+            x[idx] = special
+        return x
+    info = np.iinfo(dt)
+    lo = max(int(info.min), -100)
+    hi = min(int(info.max), 100)
+    x = rng.integers(lo, hi + 1, n).astype(dt)
+    if n:
+        x[rng.integers(0, n, max(n // 50, 1))] = 0
+    return x
+
+
+def reducer_case(rng, name):
+    rec = SIGNATURES[name]
+    args = {a[0]: a for a in rec["args"]}
+    L = _lengths(rng, 300, 4)
+    off = _offsets(L)
+    E = int(off[-1])
+    kw = {"offsets": off, "outlength": len(L)}
+    if "fromptr" in args:
+        base = args["fromptr"][1]
+        kw["fromptr"] = _values(rng, base, E)
+        if name.startswith(("awkward_reduce_max", "awkward_reduce_min")) and rng.random() < 0.5:
+            kw["fromptr"][: min(E, 5)] = kw["fromptr"][0] if E else 0
+    if "starts" in args:
+        kw["starts"] = off[:-1].copy()
+    if "identity" in args:
+        base = args["identity"][1]
+        if base in ("float", "double"):
+            kw["identity"] = float(-np.inf if "max" in name else np.inf)
+        else:
+            info = np.iinfo(NP_DTYPES[base])
+            kw["identity"] = int(info.min if "max" in name else info.max)
+    if "means" in args:
+        kw["means"] = rng.standard_normal(len(L))
+    if "n" in args:
+        kw["n"] = int(rng.choice([0, 1, 2, 3, -1]))
+    base = args["toptr"][1]
+    if name == "awkward_NumpyArray_reduce_adjust_starts_64":
+        kw["toptr"] = np.where(L > 0, off[:-1] + (L > 0) * (rng.integers(0, 1 << 20, len(L)) % np.maximum(L, 1)), -1).astype(np.int64)
+        kw["starts"] = off[:-1].copy()
+    else:
+        kw["toptr"] = np.full(len(L), 123, dtype=NP_DTYPES[base])
+    return kw
+
+
+def jagged_case(rng, name):
+    rec = SIGNATURES[name]
+    fam = rec["family"]
+    args = {a[0]: a for a in rec["args"]}
+    n = 200
+    if fam == "awkward_ListArray_getitem_jagged_apply":
+        C = NP_DTYPES[args["fromstarts"][1]]
+        L = _lengths(rng, n, 5, longs=(40,))
+        off = _offsets(L)
+        K = np.where(L > 0, rng.poisson(3, n), 0)
+        soff = _offsets(K)
+        idx = np.concatenate([rng.integers(-l, l, k) if k else np.zeros(0, np.int64) for l, k in zip(L, K)]).astype(np.int64)
+        return {"tooffsets": np.full(n + 1, 123, np.int64), "tocarry": np.full(len(idx), 123, np.int64),
+                "slicestarts": soff[:-1].copy(), "slicestops": soff[1:].copy(), "sliceouterlen": n,
+                "sliceindex": idx, "sliceinnerlen": len(idx), "fromstarts": off[:-1].astype(C),
+                "fromstops": off[1:].astype(C), "contentlen": int(off[-1])}
+    if fam == "awkward_ListArray_getitem_jagged_carrylen":
+        L = _lengths(rng, n, 5)
+        off = _offsets(L)
+        return {"carrylen": np.full(1, 123, np.int64), "slicestarts": off[:-1].copy(),
+                "slicestops": off[1:].copy(), "sliceouterlen": n}
+    if fam == "awkward_ListArray_getitem_jagged_descend":
+        C = NP_DTYPES[args["fromstarts"][1]]
+        L = _lengths(rng, n, 5)
+        off = _offsets(L) + 7
+        return {"tooffsets": np.full(n + 1, 123, np.int64), "slicestarts": off[:-1].copy(),
+                "slicestops": off[1:].copy(), "sliceouterlen": n,
+                "fromstarts": (off[:-1] * 2).astype(C), "fromstops": (off[:-1] * 2 + L).astype(C)}
+    if fam == "awkward_ListArray_getitem_jagged_expand":
+        C = NP_DTYPES[args["fromstarts"][1]]
+        js = 4
+        starts = (np.arange(n) * 9).astype(C)
+        single = _offsets(rng.poisson(2, js))
+        return {"multistarts": np.full(n * js, 123, np.int64), "multistops": np.full(n * js, 123, np.int64),
+                "singleoffsets": single, "tocarry": np.full(n * js, 123, np.int64),
+                "fromstarts": starts, "fromstops": (starts + js).astype(C), "jaggedsize": js, "length": n}
+    if fam == "awkward_ListArray_getitem_jagged_numvalid":
+        L = _lengths(rng, n, 5)
+        off = _offsets(L)
+        missing = np.where(rng.random(int(off[-1])) < 0.3, -1, np.arange(int(off[-1]))).astype(np.int64)
+        return {"numvalid": np.full(1, 123, np.int64), "slicestarts": off[:-1].copy(),
+                "slicestops": off[1:].copy(), "length": n, "missing": missing,
+                "missinglength": len(missing)}
+    if fam == "awkward_ListArray_getitem_jagged_shrink":
+        L = _lengths(rng, n, 5)
+        off = _offsets(L)
+        missing = np.where(rng.random(int(off[-1])) < 0.3, -1, np.arange(int(off[-1]))).astype(np.int64)
+        nv = int((missing >= 0).sum())
+        return {"tocarry": np.full(nv, 123, np.int64), "tosmalloffsets": np.full(n + 1, 123, np.int64),
+                "tolargeoffsets": np.full(n + 1, 123, np.int64), "slicestarts": off[:-1].copy(),
+                "slicestops": off[1:].copy(), "length": n, "missing": missing}
+    if fam == "awkward_RegularArray_getitem_jagged_expand":
+        size, length = 5, 60
+        single = _offsets(rng.poisson(3, size))
+        return {"multistarts": np.full(size * length, 123, np.int64),
+                "multistops": np.full(size * length, 123, np.int64), "singleoffsets": single,
+                "regularsize": size, "regularlength": length}
+    if fam == "awkward_ListArray_localindex":
+        C = NP_DTYPES[args["offsets"][1]]
+        L = _lengths(rng, n, 5)
+        off = _offsets(L)
+        return {"toindex": np.full(int(off[-1]), 123, np.int64), "offsets": off.astype(C), "length": n}
+    raise KeyError(fam)
+
+
+def range_cases(rng, name):
+    rec = SIGNATURES[name]
+    fam = rec["family"]
+    args = {a[0]: a for a in rec["args"]}
+    out = []
+    slices = [(1, SLICE_NONE, 1), (SLICE_NONE, SLICE_NONE, 2), (-3, SLICE_NONE, 1),
+              (SLICE_NONE, -1, 1), (SLICE_NONE, SLICE_NONE, -1), (5, 1, -2), (2, 100, 3),
+              (-100, 100, 7), (SLICE_NONE, 2, -3)]
+    if fam == "awkward_RegularArray_getitem_next_range":
+        for (rs, step, length, size, nextsize) in [(1, 1, 50, 6, 5), (5, -2, 30, 6, 3), (0, 3, 10, 9, 3)]:
+            out.append({"tocarry": np.full(length * nextsize, 123, np.int64), "regular_start": rs,
+                        "step": step, "length": length, "size": size, "nextsize": nextsize})
+        return out
+    C = NP_DTYPES[args["fromstarts"][1]]
+    for (a, b, c) in slices:
+        n = 150
+        L = _lengths(rng, n, 5, longs=(20,))
+        off = _offsets(L)
+        starts = off[:-1].astype(C)
+        stops = off[1:].astype(C)
+        if fam == "awkward_ListArray_getitem_next_range_carrylength":
+            out.append({"carrylength": np.full(1, 123, np.int64), "fromstarts": starts, "fromstops": stops,
+                        "lenstarts": n, "start": a, "stop": b, "step": c})
+        else:
+            total = int(off[-1])
+            out.append({"tooffsets": np.full(n + 1, 123, C), "tocarry": np.full(total, 123, np.int64),
+                        "fromstarts": starts, "fromstops": stops, "lenstarts": n,
+                        "start": a, "stop": b, "step": c})
+    return out
+
+
+def combinations_cases(rng, name):
+    rec = SIGNATURES[name]
+    fam = rec["family"]
+    C = NP_DTYPES[{a[0]: a for a in rec["args"]}["starts"][1]]
+    out = []
+    for n_, repl in [(2, False), (3, False), (2, True), (3, True), (1, False), (4, False)]:
+        n = 120
+        L = np.minimum(rng.poisson(4, n), 9).astype(np.int64)
+        L[rng.random(n) < 0.05] = 0
+        off = _offsets(L)
+        starts, stops = off[:-1].astype(C), off[1:].astype(C)
+        if fam == "awkward_ListArray_combinations_length":
+            out.append({"totallen": np.full(1, 123, np.int64), "tooffsets": np.full(n + 1, 123, np.int64),
+                        "n": n_, "replacement": repl, "starts": starts, "stops": stops, "length": n})
+        else:
+            tmp_total = np.zeros(1, np.int64)
+            oracle.call(oracle.load_ref(), name.replace("_combinations_64", "_combinations_length_64"),
+                        totallen=tmp_total, tooffsets=np.zeros(n + 1, np.int64), n=n_,
+                        replacement=repl, starts=starts, stops=stops, length=n)
+            total = int(tmp_total[0])
+            out.append({"tocarry": [np.full(total, 123, np.int64) for _ in range(n_)],
+                        "toindex": np.full(n_, 123, np.int64), "fromindex": np.zeros(n_, np.int64),
+                        "n": n_, "replacement": repl, "starts": starts, "stops": stops, "length": n})
+    return out
+
+
+def make_random():
+    rng = np.random.default_rng(20241203)
+    ref = oracle.load_ref()
+    if ref is None:
+        raise SystemExit("awkward-cpp CPU kernels not built (oracle/build.py)")
+    manifest = []
+    arrays = {}
+    for name, rec in SIGNATURES.items():
+        fam = rec["family"]
+        if fam.startswith(("awkward_reduce", "awkward_NumpyArray_reduce")):
+            cases = [reducer_case(rng, name)]
+        elif "next_range" in fam:
+            cases = range_cases(rng, name)
+        elif "combinations" in fam:
+            cases = combinations_cases(rng, name)
+        else:
+            cases = [jagged_case(rng, name)]
+        for kw in cases:
+            inputs = {k: (v.copy() if isinstance(v, np.ndarray) else [r.copy() for r in v] if isinstance(v, list) else v)
+                      for k, v in kw.items()}
+            err = oracle.call(ref, name, **kw)
+            i = len(manifest)
+            entry = {"name": name, "scalars": {}, "arrays": [], "lists": {}, "outs": [], "error": err[0],
+                     "identity": int(err[1]), "attempt": int(err[2])}
+            for (an, base, d, depth, _c, _r) in rec["args"]:
+                v = inputs[an]
+                if depth == 0:
+                    entry["scalars"][an] = v if not isinstance(v, (np.generic,)) else v.item()
+                elif depth == 1:
+                    arrays[f"{i}:in:{an}"] = v
+                    entry["arrays"].append(an)
+                    if d == "out":
+                        arrays[f"{i}:out:{an}"] = kw[an]
+                        entry["outs"].append(an)
+                else:
+                    entry["lists"][an] = len(v)
+                    for r, row in enumerate(v):
+                        arrays[f"{i}:in:{an}:{r}"] = row
+                        arrays[f"{i}:out:{an}:{r}"] = kw[an][r]
+                    entry["outs"].append(an)
+            manifest.append(entry)
+    arrays["manifest"] = np.frombuffer(json.dumps(manifest).encode(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, "ref_random.npz"), **arrays)
+    return len(manifest)
+
+
+if __name__ == "__main__":
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("AWKWARD_SRC", "/root/reference")
+    from oracle import build
+
+    build.build_oracle()
+    build.build_ref(src)
+    print("unit tests:", extract_unit_tests(src))
+    print("random cases:", make_random())
