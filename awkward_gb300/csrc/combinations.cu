@@ -1,0 +1,205 @@
+// combinations.cu -- n-tuples of the elements of each list.
+//
+//   awkward_ListArray_combinations_length  awkward_ListArray_combinations_length.cpp:8-45
+//   awkward_ListArray_combinations         awkward_ListArray_combinations.cpp:9-33 with the
+//                                          enumeration of kernel-utils.cpp:41-80
+//
+// The CPU enumerates each list's tuples depth-first in lexicographic order.
+// Here every output slot is produced independently: a list tile scans the
+// per-list tuple counts (decoupled look-back), then consecutive threads take
+// consecutive output slots, find their list by binary search and unrank the
+// slot's lexicographic rank into the tuple (combinatorial number system:
+// choose each position by binary search over "tuples whose next element is
+// below v" = C(s-lo, rem) - C(s-v, rem)).  With replacement the
+// non-decreasing tuple over s elements is the strictly increasing tuple over
+// s+n-1 elements with position p shifted down by p.  All n output arrays are
+// written coalesced.
+#include "list_tile.cuh"
+
+using namespace gb;
+
+namespace {
+
+constexpr int kMaxPtrs = 32;
+
+// The CPU's per-list count, including its arithmetic (no overflow check).
+__device__ __forceinline__ long long combinations_count(long long size, long long n,
+                                                        bool replacement) {
+  if (replacement) size += n - 1;
+  long long thisn = n;
+  if (thisn > size) return 0;
+  if (thisn == size) return 1;
+  if (thisn * 2 > size) thisn = size - thisn;
+  long long len = size;
+  for (long long j = 2; j <= thisn; j++) {
+    len *= (size - j + 1);
+    len /= j;
+  }
+  return len;
+}
+
+// C(m, k) by the exact multiplicative recurrence; 0 outside 0 <= k <= m.
+__device__ __forceinline__ long long binom(long long m, long long k) {
+  if (k < 0 || m < 0 || k > m) return 0;
+  if (k > m - k) k = m - k;
+  if (k == 0) return 1;
+  if (k == 1) return m;
+  if (k == 2) return m * (m - 1) / 2;
+  long long r = 1;
+  for (long long j = 1; j <= k; j++) r = r * (m - k + j) / j;
+  return r;
+}
+
+template <class C>
+__global__ void __launch_bounds__(kTileBlock)
+    combinations_length_kernel(int64_t* __restrict__ totallen, int64_t* __restrict__ tooffsets,
+                               long long n, bool replacement, const C* __restrict__ starts,
+                               const C* __restrict__ stops, long long length, long long ntiles,
+                               ScanTiles st, uint64_t inv, uint64_t* err) {
+  __shared__ TileSmem sm;
+  const long long tile = tile_claim(sm, st);
+  const long long l0 = tile * kTileLists;
+  long long cnt[kTileLPT];
+#pragma unroll
+  for (int r = 0; r < kTileLPT; r++) {
+    const long long i = l0 + threadIdx.x * kTileLPT + r;
+    cnt[r] = i < length ? combinations_count((long long)(stops[i] - starts[i]), n, replacement) : 0;
+  }
+  const long long prefix = tile_scan(sm, st, tile, cnt, inv, err);
+  for (int li = threadIdx.x; li < kTileLists; li += kTileBlock) {
+    const long long i = l0 + li;
+    if (i < length) tooffsets[i + 1] = prefix + sm.loc[li + 1];
+  }
+  if (tile == 0 && threadIdx.x == 0) tooffsets[0] = 0;
+  if (tile == ntiles - 1 && threadIdx.x == 0) totallen[0] = prefix + sm.total;
+}
+
+template <class C>
+__global__ void __launch_bounds__(kTileBlock)
+    combinations_kernel(int64_t** __restrict__ tocarry, int64_t* __restrict__ toindex,
+                        long long n, bool replacement, const C* __restrict__ starts,
+                        const C* __restrict__ stops, long long length, long long ntiles,
+                        ScanTiles st, uint64_t inv, uint64_t* err) {
+  __shared__ TileSmem sm;
+  __shared__ long long s_start[kTileLists];
+  __shared__ long long s_size[kTileLists];
+  __shared__ int64_t* s_ptr[kMaxPtrs];
+  const long long tile = tile_claim(sm, st);
+  const long long l0 = tile * kTileLists;
+  if (threadIdx.x < kMaxPtrs && threadIdx.x < n) s_ptr[threadIdx.x] = tocarry[threadIdx.x];
+  long long cnt[kTileLPT];
+#pragma unroll
+  for (int r = 0; r < kTileLPT; r++) {
+    const int li = threadIdx.x * kTileLPT + r;
+    const long long i = l0 + li;
+    long long c = 0;
+    if (i < length) {
+      const long long s0 = (long long)starts[i];
+      const long long size = (long long)(stops[i] - starts[i]);
+      c = combinations_count(size, n, replacement);
+      s_start[li] = s0;
+      s_size[li] = replacement ? size + n - 1 : size;
+    }
+    cnt[r] = c;
+  }
+  const long long prefix = tile_scan(sm, st, tile, cnt, inv, err);
+  const long long total = sm.total;
+  if (tile == ntiles - 1 && threadIdx.x < n)
+    for (long long p = threadIdx.x; p < n; p += kTileBlock) toindex[p] = prefix + total;
+  if (n <= 0) return;
+  for (long long q = threadIdx.x; q < total; q += kTileBlock) {
+    const int r = tile_find(sm, q);
+    long long rank = q - sm.loc[r];
+    const long long s = s_size[r];
+    const long long base = s_start[r];
+    const long long out = prefix + q;
+    if (n == 2) {
+      // first element: largest v with C(s,2) - C(s-v,2) <= rank
+      const long long tot = s * (s - 1) / 2;
+      long long lo = 0, hi = s - 2;
+      while (lo < hi) {
+        long long mid = (lo + hi + 1) >> 1;
+        long long m = s - mid;
+        if (tot - m * (m - 1) / 2 <= rank) lo = mid;
+        else hi = mid - 1;
+      }
+      const long long m = s - lo;
+      const long long a = lo;
+      const long long b2 = lo + 1 + (rank - (tot - m * (m - 1) / 2));
+      s_ptr[0][out] = base + a;
+      s_ptr[1][out] = base + (replacement ? b2 - 1 : b2);
+      continue;
+    }
+    long long lo = 0;
+    for (long long p = 0; p < n; p++) {
+      const long long rem = n - p;
+      const long long here = binom(s - lo, rem);
+      long long vlo = lo, vhi = s - rem;
+      while (vlo < vhi) {
+        long long mid = (vlo + vhi + 1) >> 1;
+        if (here - binom(s - mid, rem) <= rank) vlo = mid;
+        else vhi = mid - 1;
+      }
+      rank -= here - binom(s - vlo, rem);
+      int64_t* dst = p < kMaxPtrs ? s_ptr[p] : tocarry[p];
+      dst[out] = base + (replacement ? vlo - p : vlo);
+      lo = vlo + 1;
+    }
+  }
+}
+
+}  // namespace
+
+#define GB_COMB_LENGTH(NAME, C)                                                                 \
+  GB_EXPORT int NAME(int64_t* totallen, int64_t* tooffsets, int64_t n, bool replacement,       \
+                     const C* starts, const C* stops, int64_t length, uint64_t invocation_index, \
+                     uint64_t* err_code, void* stream) {                                        \
+    cudaStream_t s = (cudaStream_t)stream;                                                      \
+    if (length <= 0) {                                                                          \
+      cudaError_t e = cudaMemsetAsync(tooffsets, 0, sizeof(int64_t), s);                        \
+      if (e != cudaSuccess) return (int)e;                                                      \
+      return (int)cudaMemsetAsync(totallen, 0, sizeof(int64_t), s);                             \
+    }                                                                                           \
+    const long long nt = tile_count(length);                                                    \
+    ScanTiles st;                                                                               \
+    void* base = nullptr;                                                                       \
+    cudaError_t e = scan_tiles_alloc(&st, &base, nt, s);                                        \
+    if (e != cudaSuccess) return (int)e;                                                        \
+    combinations_length_kernel<C><<<(unsigned)nt, kTileBlock, 0, s>>>(                          \
+        totallen, tooffsets, n, replacement, starts, stops, length, nt, st, invocation_index,   \
+        err_code);                                                                              \
+    e = cudaGetLastError();                                                                     \
+    cudaError_t f = scratch_free(base, s);                                                      \
+    return (int)(e != cudaSuccess ? e : f);                                                     \
+  }
+GB_COMB_LENGTH(awkward_ListArray32_combinations_length_64, int32_t)
+GB_COMB_LENGTH(awkward_ListArrayU32_combinations_length_64, uint32_t)
+GB_COMB_LENGTH(awkward_ListArray64_combinations_length_64, int64_t)
+
+// toindex must hold n entries; it receives the total number of tuples per
+// position (the CPU's final counters).  fromindex is the CPU's scratch
+// cursor and is not used.
+#define GB_COMB(NAME, C)                                                                       \
+  GB_EXPORT int NAME(int64_t** tocarry, int64_t* toindex, int64_t* fromindex, int64_t n,       \
+                     bool replacement, const C* starts, const C* stops, int64_t length,        \
+                     uint64_t invocation_index, uint64_t* err_code, void* stream) {            \
+    (void)fromindex;                                                                           \
+    cudaStream_t s = (cudaStream_t)stream;                                                     \
+    if (n <= 0) return 0;                                                                      \
+    if (length <= 0) return (int)cudaMemsetAsync(toindex, 0, sizeof(int64_t) * n, s);          \
+    const long long nt = tile_count(length);                                                   \
+    ScanTiles st;                                                                              \
+    void* base = nullptr;                                                                      \
+    cudaError_t e = scan_tiles_alloc(&st, &base, nt, s);                                       \
+    if (e != cudaSuccess) return (int)e;                                                       \
+    combinations_kernel<C><<<(unsigned)nt, kTileBlock, 0, s>>>(tocarry, toindex, n,            \
+                                                               replacement, starts, stops,     \
+                                                               length, nt, st,                 \
+                                                               invocation_index, err_code);    \
+    e = cudaGetLastError();                                                                    \
+    cudaError_t f = scratch_free(base, s);                                                     \
+    return (int)(e != cudaSuccess ? e : f);                                                    \
+  }
+GB_COMB(awkward_ListArray32_combinations_64, int32_t)
+GB_COMB(awkward_ListArrayU32_combinations_64, uint32_t)
+GB_COMB(awkward_ListArray64_combinations_64, int64_t)

@@ -1,0 +1,97 @@
+"""GPU parity: every entry point against awkward's golden vectors and awkward-cpp's outputs.
+
+Integer, index, boolean, count, offsets, carry and combinations outputs and
+max/min values must be bit-identical.  Order-dependent floating-point sums
+(sum, prod, sum of squares/powers, centered sum of squares) must be within
+4*n*eps*sum|term| of awkward-cpp's left-to-right result, per list (n = list
+length, eps of the output type); non-finite results must match exactly.
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+import golden_cases as gc
+from gpu_util import run_gpu
+
+pytestmark = pytest.mark.gpu
+
+UNIT = gc.unit_case_ids()
+RANDOM = gc.random_case_ids()
+
+
+def _terms(name, kw):
+    """|term| per element as the reducer sees it (float64), for the error bound."""
+    from awkward_gb300._signatures import SIGNATURES
+
+    fam = SIGNATURES[name]["family"]
+    x = np.asarray(kw["fromptr"]).astype(np.float64)
+    if fam in ("awkward_reduce_sum",):
+        return np.abs(x)
+    if fam == "awkward_reduce_sumofsquares":
+        return x * x
+    if fam == "awkward_reduce_centered_sumofsquares":
+        off = np.asarray(kw["offsets"])
+        parents = np.repeat(np.arange(len(off) - 1), np.diff(off))
+        d = x[off[0]:off[-1]] - np.asarray(kw["means"])[parents]
+        out = np.zeros_like(x)
+        out[off[0]:off[-1]] = d * d
+        return out
+    if fam == "awkward_reduce_sumofpowers":
+        with np.errstate(all="ignore"):
+            return np.abs(np.power(x, float(kw["n"])))
+    return np.abs(x)
+
+
+def check_float_sum_like(name, kw, got, exp):
+    from awkward_gb300._signatures import SIGNATURES
+
+    fam = SIGNATURES[name]["family"]
+    out_t = SIGNATURES[name]["args"][0][1]
+    eps = np.finfo(np.float32 if out_t == "float" else np.float64).eps
+    off = np.asarray(kw["offsets"])
+    got = np.asarray(got)[: len(exp)].astype(np.float64)
+    exp = np.asarray(exp).astype(np.float64)
+    finite = np.isfinite(exp)
+    np.testing.assert_array_equal(np.isnan(got), np.isnan(exp))
+    np.testing.assert_array_equal(got[np.isinf(exp)], exp[np.isinf(exp)])
+    if fam == "awkward_reduce_prod":
+        n = np.diff(off).astype(np.float64)
+        tiny = np.finfo(np.float32 if out_t == "float" else np.float64).tiny
+        bound = 4 * np.maximum(n, 1) * eps * np.abs(exp) + 64 * tiny
+    else:
+        with np.errstate(all="ignore"):
+            t = _terms(name, kw)
+            cs = np.concatenate([[0.0], np.cumsum(t)])
+            scale = cs[off[1:]] - cs[off[:-1]]
+        n = np.diff(off).astype(np.float64)
+        bound = 4 * np.maximum(n, 1) * eps * scale
+    err = np.abs(got - exp)
+    bad = finite & ~(err <= bound)
+    assert not bad.any(), (name, np.nonzero(bad)[0][:5], got[bad][:5], exp[bad][:5], bound[bad][:5])
+
+
+@pytest.mark.parametrize("name,index", UNIT, ids=[f"{n}-{i}" for n, i in UNIT])
+def test_gpu_kernel_test_data(name, index):
+    kw, expected, message = gc.unit_case(name, index)
+    outs, err = run_gpu(name, kw)
+    if message is not None:
+        assert err is not None and err.startswith(message), (err, message)
+        return
+    assert err is None, err
+    gc.assert_outputs_equal(name, outs, expected, exact=True)
+
+
+@pytest.mark.parametrize("name,index", RANDOM, ids=[f"{n}-{i}" for n, i in RANDOM])
+def test_gpu_matches_awkward_cpp(name, index):
+    _name, kw, expected, error = gc.random_case(index)
+    outs, err = run_gpu(name, kw)
+    if error is not None:
+        assert err is not None and err.startswith(error), (err, error)
+        return
+    assert err is None, err
+    if gc.is_float_sum_like(name):
+        check_float_sum_like(name, kw, outs["toptr"], expected["toptr"])
+    else:
+        gc.assert_outputs_equal(name, outs, expected, exact=True)
