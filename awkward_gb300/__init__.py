@@ -8,7 +8,7 @@ the names and argument lists of awkward's kernel-specification.yml.
 Entry points for Python callers:
 
 * ``backend()`` -- the kernel table ``backend[(family, *dtypes)]`` over torch
-  CUDA tensors, with awkward's error protocol (see ``backend.py``);
+  CUDA tensors, with awkward's error protocol (see ``kernel_table.py``);
 * ``cupy_adapter.install()`` -- registers the same kernels in awkward's own
   cupy kernel table;
 * ``build()`` -- compiles the library in-tree with nvcc.
@@ -29,6 +29,6 @@ def build(force=False, verbose=False):
 
 def backend():
     """The process-wide kernel table over torch CUDA tensors."""
-    from .backend import backend as _backend
+    from .kernel_table import backend as _backend
 
     return _backend()

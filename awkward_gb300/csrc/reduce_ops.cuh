@@ -209,21 +209,20 @@ struct CenteredSumSqOp {
 };
 
 // ---------------------------------------------------------------- launcher
-constexpr int kReduceBlock = 256;
-constexpr int kReduceIPT = 8;
 constexpr int kFixupBlock = 1024;
 
-template <class Op, int BLOCK, int IPT>
+template <class Op>
 struct SegReduceConfig {
+  using Sm = SegSmem<store_t<typename Op::In>, typename Op::Acc>;
   static int blocks_per_sm() {
     static std::once_flag once;
     static int bps = 1;
     std::call_once(once, [] {
-      using L = SegReduceLayout<BLOCK, IPT, store_t<typename Op::In>>;
-      auto k = seg_reduce_kernel<Op, BLOCK, IPT>;
-      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::bytes);
+      auto k = seg_reduce_kernel<Op>;
+      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sm));
       int n = 0;
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, BLOCK, L::bytes) != cudaSuccess ||
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kSegThreads, sizeof(Sm)) !=
+              cudaSuccess ||
           n < 1)
         n = 1;
       bps = n;
@@ -232,29 +231,30 @@ struct SegReduceConfig {
   }
 };
 
-// Launch the segmented reduction of `nlists` lists on `stream`.  Returns the
-// launch status; data never travel to the host.
-template <class Op, int BLOCK = kReduceBlock, int IPT = kReduceIPT>
+// Launch the segmented reduction of `nlists` lists on `stream`: the
+// persistent merge-path kernel, then the one-block cross-CTA fix-up.
+// Returns the launch status; data never travel to the host.
+template <class Op>
 cudaError_t launch_seg_reduce(const Op& op, const store_t<typename Op::In>* x,
                               const int64_t* offsets, long long nlists, typename Op::Out* out,
                               uint64_t inv, uint64_t* err, cudaStream_t stream,
                               int grid_override = 0) {
   if (nlists <= 0) return cudaSuccess;
-  using L = SegReduceLayout<BLOCK, IPT, store_t<typename Op::In>>;
   using Rec = CtaRecord<typename Op::Acc>;
-  int G = grid_override > 0 ? grid_override
-                            : device_sm_count() * SegReduceConfig<Op, BLOCK, IPT>::blocks_per_sm();
+  using Sm = typename SegReduceConfig<Op>::Sm;
+  const int G = grid_override > 0 ? grid_override
+                                  : device_sm_count() * SegReduceConfig<Op>::blocks_per_sm();
   void* rec = nullptr;
   cudaError_t e = scratch_alloc(&rec, (size_t)G * sizeof(Rec), stream);
   if (e != cudaSuccess) return e;
   const int use_tma = ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(offsets)) &
                        15) == 0;
-  seg_reduce_kernel<Op, BLOCK, IPT><<<G, BLOCK, L::bytes, stream>>>(
+  seg_reduce_kernel<Op><<<G, kSegThreads, sizeof(Sm), stream>>>(
       op, x, offsets, nlists, out, reinterpret_cast<Rec*>(rec), G, use_tma, inv, err);
   e = cudaGetLastError();
   if (e == cudaSuccess) {
     seg_reduce_fixup_kernel<Op, kFixupBlock><<<1, kFixupBlock, 0, stream>>>(
-        op, offsets, nlists, out, reinterpret_cast<const Rec*>(rec), G, L::IPC);
+        op, offsets, nlists, out, reinterpret_cast<const Rec*>(rec), G, kSegIPC);
     e = cudaGetLastError();
   }
   cudaError_t f = scratch_free(rec, stream);

@@ -8,23 +8,24 @@
 // j in [offsets[0], offsets[nlists]).  Consuming an element accumulates it
 // into the current list; consuming a list end emits that list's result.  The
 // merged sequence has D = nlists + E items.  A persistent grid of G CTAs
-// splits D into G equal diagonal ranges (perfect balance for any length
-// distribution: empty lists, Poisson, heavy tails, one giant list), each
-// CTA locating its two ends with a warp-wide 32-ary merge-path search in
-// global memory.
+// splits D into equal diagonal ranges (perfect balance for any length
+// distribution: empty lists, Poisson, heavy tails, one giant list); each CTA
+// locates its two ends with a warp-wide 32-ary merge-path search in global
+// memory.
 //
-// Inside a CTA the two streams are read strictly sequentially into two
-// shared-memory rings (offsets ring and element ring), each kept filled to
-// one chunk ahead of the cursor.  Refills are 1-D TMA bulk copies
-// (cp.async.bulk, 16-byte aligned interior; ragged edges by plain loads)
-// issued for chunk c+1 before chunk c is reduced, so HBM traffic is one pass
-// over offsets and content with no re-reads.  Each chunk is IPC = BLOCK*IPT
-// merge items; every thread walks IPT consecutive items (found by a binary
-// search in shared memory), accumulates its lists with the reducer policy,
-// writes the lists that end inside its range, and a block-wide segmented
-// scan stitches lists that cross threads.  Lists that cross CTAs leave one
-// head and one tail record per CTA; a one-block fix-up kernel combines them
-// with a segmented scan in CTA order.  No CTA ever waits on another.
+// Inside a CTA, one producer warp streams the CTA's slices of `offsets` and
+// of the content into two shared-memory rings of fixed-size stages with 1-D
+// TMA bulk copies (cp.async.bulk of the 16-byte aligned interior; ragged
+// head and tail by plain loads), guarded by full/empty mbarrier pairs, so
+// loads run several chunks ahead of the reduction.  Eight consumer warps
+// reduce chunks of IPC = 256*IPT merge items: they convert the chunk's list
+// ends into a linear int32 window (relative to the chunk's first element),
+// every thread locates its IPT items by binary search in that window and
+// walks them, a block-wide segmented scan stitches lists that cross
+// threads, and finished stages are handed back to the producer.  HBM
+// traffic is one pass over offsets and content.  Lists that cross CTAs leave
+// one head and one tail record per CTA; a one-block fix-up kernel combines
+// them with a segmented scan in CTA order.  No CTA ever waits on another.
 //
 // Combination order is always earlier-then-later, so order-sensitive
 // reducers (max/min/argmax/argmin tie and NaN rules) are bit-exact with the
@@ -59,55 +60,54 @@ struct CtaRecord {
   int pad;
 };
 
-template <int BLOCK, int IPT, class Store>
-struct SegReduceLayout {
-  static constexpr int IPC = BLOCK * IPT;
-  static constexpr int RE = 2 * IPC;        // element ring entries (power of two)
-  static constexpr int RL = 2 * IPC + 16;   // offsets ring entries (even)
-  static constexpr size_t off_ring = 0;
-  static constexpr size_t elem_ring = (size_t)RL * 8;
-  static constexpr size_t elem_bytes = ((size_t)RE * sizeof(Store) + 15) / 16 * 16;
-  static constexpr size_t misc = elem_ring + elem_bytes;  // barrier + small shared state
-  static constexpr size_t bytes = misc + 256;
-  static_assert((RE & (RE - 1)) == 0, "element ring must be a power of two");
-  static_assert(((size_t)RE * sizeof(Store)) % 16 == 0, "ring must be a 16-byte multiple");
+constexpr int kConsumers = 256;  // consumer threads (8 warps)
+constexpr int kProducerWarp = kConsumers / 32;
+constexpr int kSegThreads = kConsumers + 32;
+constexpr int kSegIPT = 8;
+constexpr int kSegIPC = kConsumers * kSegIPT;  // merge items per chunk
+constexpr int kEStage = 512;                   // elements per content stage
+constexpr int kEStages = 8;                    // content ring: 4096 elements
+constexpr int kOStage = 256;                   // offsets per offsets stage
+constexpr int kOStages = 12;                   // offsets ring: 3072 entries
+constexpr int kLendBig = 0x7fffffff;
+static_assert(kEStages * kEStage >= kSegIPC + kEStage, "content ring too small");
+static_assert(kOStages * kOStage >= kSegIPC + 1 + kOStage, "offsets ring too small");
+
+template <class Store, class Acc>
+struct SegSmem {
+  int64_t oring[kOStages * kOStage];
+  Store ering[kEStages * kEStage];
+  int lend[kSegIPC + 1];  // chunk-local list ends (element position relative to cj)
+  SegVal<Acc> scan[kConsumers / 32 + 1];
+  SegVal<Acc> carry;
+  uint64_t full_e[kEStages], empty_e[kEStages];
+  uint64_t full_o[kOStages], empty_o[kOStages];
+  long long coords[4];
+  long long lstart0;  // start of list ci relative to cj
+  int kend;
+  int head_pending;
 };
 
-// Fill ring slots for global indices [g0, g1) of `src` (one thread).  Returns
-// the bytes issued as TMA bulk copies (to be announced on the mbarrier
-// before the copies are issued: call with issue=false first).
-template <class T, int R>
-__device__ __forceinline__ uint32_t ring_fill(T* ring, const T* src, long long g0, long long g1,
-                                              uint64_t* bar, bool use_tma, bool issue) {
-  constexpr int A = 16 / (int)sizeof(T);  // elements per 16 bytes
-  uint32_t bytes = 0;
-  long long a = g0;
-  while (a < g1) {
-    long long wrap = (a / R + 1) * (long long)R;
-    long long b = g1 < wrap ? g1 : wrap;
-    long long a16 = use_tma ? (a + A - 1) / A * A : b;
-    long long b16 = use_tma ? b / A * A : b;
-    if (a16 < b16) {
-      uint32_t n = (uint32_t)((b16 - a16) * (long long)sizeof(T));
-      if (issue) bulk_g2s(ring + (a16 % R), src + a16, n, bar);
-      bytes += n;
-    } else {
-      a16 = b;
-      b16 = b;
-    }
-    if (issue) {
-      for (long long g = a; g < (a16 < b ? a16 : b); g++) ring[g % R] = src[g];
-      for (long long g = (b16 > a ? b16 : a); g < b; g++) ring[g % R] = src[g];
-    }
-    a = b;
-  }
-  return bytes;
+__device__ __forceinline__ void consumer_sync() {
+  asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
 }
 
-// Cooperative plain-load fill (used when a base pointer is not 16-byte aligned).
-template <int BLOCK, class T, int R>
-__device__ __forceinline__ void ring_fill_coop(T* ring, const T* src, long long g0, long long g1) {
-  for (long long g = g0 + threadIdx.x; g < g1; g += BLOCK) ring[g % R] = src[g];
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n"
+      ".reg .pred p;\n"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
 }
 
 // Merge-path split of diagonal d in global memory (one warp).  Returns the
@@ -119,44 +119,69 @@ __device__ __forceinline__ long long mp_search_global(const int64_t* __restrict_
   long long lo = d - E > 0 ? d - E : 0;
   long long hi = d < nlists ? d : nlists;  // answer in [lo, hi]
   while (hi - lo > 32) {
-    long long step = (hi - lo) / 32;
-    long long k = lo + (long long)lane * step;
-    bool p = (k + (offsets[k + 1] - e0)) < d;
-    unsigned m = __ballot_sync(0xffffffffu, p);
-    int cnt = __popc(m);
-    long long k_prev = lo + (long long)(cnt - 1) * step;
-    long long k_next = lo + (long long)cnt * step;
-    long long nlo = cnt > 0 ? k_prev + 1 : lo;
-    long long nhi = cnt < 32 ? k_next : hi;
+    const long long step = (hi - lo) / 32;
+    const long long k = lo + (long long)lane * step;
+    const bool p = (k + (offsets[k + 1] - e0)) < d;
+    const unsigned msk = __ballot_sync(0xffffffffu, p);
+    const int cnt = __popc(msk);
+    const long long nlo = cnt > 0 ? lo + (long long)(cnt - 1) * step + 1 : lo;
+    const long long nhi = cnt < 32 ? lo + (long long)cnt * step : hi;
     lo = nlo;
     hi = nhi;
   }
-  long long k = lo + lane;
-  bool p = (k < hi) && ((k + (offsets[k + 1] - e0)) < d);
-  unsigned m = __ballot_sync(0xffffffffu, p);
-  return lo + __popc(m);
+  const long long k = lo + lane;
+  const bool p = (k < hi) && ((k + (offsets[k + 1] - e0)) < d);
+  const unsigned msk = __ballot_sync(0xffffffffu, p);
+  return lo + __popc(msk);
 }
 
-template <class Op, int BLOCK, int IPT>
-__global__ void __launch_bounds__(BLOCK)
+// Producer warp: copy global [lo, hi) of `src` into ring slot `slot` (the
+// slot holds global [stage_lo, stage_lo + STAGE)), completing barrier
+// `full`.  With TMA the 16-byte aligned interior is one bulk copy and the
+// ragged head and tail (each shorter than 16 bytes) are plain loads issued
+// before the arrive, which releases them.
+template <class T, int STAGE>
+__device__ __forceinline__ void produce_stage(T* ring, const T* src, long long stage_lo,
+                                              long long lo, long long hi, int slot,
+                                              uint64_t* full, bool use_tma) {
+  T* slot_base = ring + (size_t)slot * STAGE;
+  const int lane = threadIdx.x & 31;
+  if (use_tma) {
+    constexpr int A = 16 / (int)sizeof(T);
+    long long a16 = (lo + A - 1) / A * A;
+    long long b16 = hi / A * A;
+    if (a16 >= b16) a16 = b16 = hi;
+    if (lane == 0) {
+      const uint32_t bytes = (uint32_t)((b16 - a16) * (long long)sizeof(T));
+      for (long long g = lo; g < a16; g++) slot_base[g - stage_lo] = src[g];
+      for (long long g = b16; g < hi; g++) slot_base[g - stage_lo] = src[g];
+      mbar_arrive_expect_tx(full, bytes);
+      if (bytes) bulk_g2s(slot_base + (a16 - stage_lo), src + a16, bytes, full);
+    }
+  } else {
+    for (long long g = lo + lane; g < hi; g += 32) slot_base[g - stage_lo] = src[g];
+    __syncwarp();
+    if (lane == 0) mbar_arrive(full);
+  }
+}
+
+template <class Op>
+__global__ void __launch_bounds__(kSegThreads)
     seg_reduce_kernel(Op op, const store_t<typename Op::In>* __restrict__ x,
                       const int64_t* __restrict__ offsets, long long nlists,
                       typename Op::Out* __restrict__ out, CtaRecord<typename Op::Acc>* records,
-                      int G, int use_tma, uint64_t inv, uint64_t* err) {
+                      int G, int use_tma_i, uint64_t inv, uint64_t* err) {
   using Acc = typename Op::Acc;
   using Store = store_t<typename Op::In>;
-  using L = SegReduceLayout<BLOCK, IPT, Store>;
   using V = SegVal<Acc>;
-  constexpr int IPC = L::IPC, RE = L::RE, RL = L::RL;
-  constexpr int NW = BLOCK / 32;
+  using Sm = SegSmem<Store, Acc>;
+  constexpr int IPC = kSegIPC, IPT = kSegIPT;
+  constexpr int RE = kEStages * kEStage;
+  constexpr int RO = kOStages * kOStage;
 
-  extern __shared__ __align__(128) unsigned char smem[];
-  int64_t* oring = reinterpret_cast<int64_t*>(smem + L::off_ring);
-  Store* xring = reinterpret_cast<Store*>(smem + L::elem_ring);
-  uint64_t* bar = reinterpret_cast<uint64_t*>(smem + L::misc);
-  long long* sh = reinterpret_cast<long long*>(smem + L::misc + 16);  // 6 words
-  __shared__ V scan_smem[NW + 1];
-  __shared__ V cta_carry;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  Sm& sm = *reinterpret_cast<Sm*>(smem_raw);
+  const bool use_tma = use_tma_i != 0;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const long long e0 = offsets[0];
@@ -169,187 +194,244 @@ __global__ void __launch_bounds__(BLOCK)
   const long long d_begin = D * b / Geff, d_end = D * (b + 1) / Geff;
 
   if (warp < 2) {
-    long long d = warp == 0 ? d_begin : d_end;
-    long long i = mp_search_global(offsets, nlists, e0, E, d);
+    const long long d = warp == 0 ? d_begin : d_end;
+    const long long i = mp_search_global(offsets, nlists, e0, E, d);
     if (lane == 0) {
-      sh[warp * 2] = i;
-      sh[warp * 2 + 1] = e0 + (d - i);
+      sm.coords[warp * 2] = i;
+      sm.coords[warp * 2 + 1] = e0 + (d - i);
     }
   }
   if (tid == 0) {
-    mbar_init(bar, 1);
+    for (int s = 0; s < kEStages; s++) {
+      mbar_init(&sm.full_e[s], 1);
+      mbar_init(&sm.empty_e[s], 1);
+    }
+    for (int s = 0; s < kOStages; s++) {
+      mbar_init(&sm.full_o[s], 1);
+      mbar_init(&sm.empty_o[s], 1);
+    }
     fence_barrier_init();
     records[b].head_list = -1;
   }
   __syncthreads();
-  const long long I0 = sh[0], J0 = sh[1], I1 = sh[2], J1 = sh[3];
+  const long long I0 = sm.coords[0], J0 = sm.coords[1], I1 = sm.coords[2], J1 = sm.coords[3];
+  // Stage grids: content stage s holds [EB + s*kEStage, ...) and offsets stage
+  // t holds [OB + t*kOStage, ...); both bases are multiples of the stage size.
+  const long long EB = J0 / kEStage * kEStage;
+  const long long OB = I0 / kOStage * kOStage;
+  const long long ne_st = J1 > J0 ? (J1 - EB + kEStage - 1) / kEStage : 0;
+  const long long no_st = (I1 + 1 - OB + kOStage - 1) / kOStage;
 
-  // initial windows: offsets [I0, min(I0+IPC, I1)], elements [J0, min(J0+IPC, J1))
-  long long ohi = (I0 + IPC < I1 ? I0 + IPC : I1) + 1;  // exclusive fill end of offsets
-  long long ehi = J0 + IPC < J1 ? J0 + IPC : J1;        // exclusive fill end of elements
-  uint32_t phase = 0;
-  if (use_tma) {
-    if (tid == 0) {
-      uint32_t nb = ring_fill<int64_t, RL>(oring, offsets, I0, ohi, bar, true, false) +
-                    ring_fill<Store, RE>(xring, x, J0, ehi, bar, true, false);
-      mbar_arrive_expect_tx(bar, nb);
-      ring_fill<int64_t, RL>(oring, offsets, I0, ohi, bar, true, true);
-      ring_fill<Store, RE>(xring, x, J0, ehi, bar, true, true);
+  if (warp == kProducerWarp) {
+    // ------------------------------------------------------------ producer
+    long long se = 0, so = 0;
+    uint32_t spins = 0;
+    while (se < ne_st || so < no_st) {
+      bool progressed = false;
+      if (se < ne_st) {
+        const int slot = (int)(se % kEStages);
+        const long long round = se / kEStages;
+        int ok = round == 0;
+        if (!ok && lane == 0) ok = mbar_test(&sm.empty_e[slot], (uint32_t)((round - 1) & 1));
+        if (__shfl_sync(0xffffffffu, ok, 0)) {
+          const long long st = EB + se * kEStage;
+          const long long lo = st > J0 ? st : J0;  // never read before the CTA's first element
+          const long long hi = st + kEStage < J1 ? st + kEStage : J1;
+          produce_stage<Store, kEStage>(sm.ering, x, st, lo, hi, slot, &sm.full_e[slot],
+                                        use_tma);
+          se++;
+          progressed = true;
+        }
+      }
+      if (so < no_st) {
+        const int slot = (int)(so % kOStages);
+        const long long round = so / kOStages;
+        int ok = round == 0;
+        if (!ok && lane == 0) ok = mbar_test(&sm.empty_o[slot], (uint32_t)((round - 1) & 1));
+        if (__shfl_sync(0xffffffffu, ok, 0)) {
+          const long long st = OB + so * kOStage;
+          const long long hi = st + kOStage < I1 + 1 ? st + kOStage : I1 + 1;
+          produce_stage<int64_t, kOStage>(sm.oring, offsets, st, st, hi, slot, &sm.full_o[slot],
+                                          use_tma);
+          so++;
+          progressed = true;
+        }
+      }
+      if (progressed) {
+        spins = 0;
+      } else {
+        if (++spins > kSpinLimit) {
+          if (lane == 0) raise_error(err, inv, GB_MSG_TIMEOUT);
+          break;
+        }
+        __nanosleep(64);
+      }
     }
-  } else {
-    ring_fill_coop<BLOCK, int64_t, RL>(oring, offsets, I0, ohi);
-    ring_fill_coop<BLOCK, Store, RE>(xring, x, J0, ehi);
+    return;
   }
 
-  const bool head_pending0 = offsets[I0] < J0;  // list I0 has elements in earlier CTAs
+  // -------------------------------------------------------------- consumers
   if (tid == 0) {
-    cta_carry.acc = op.identity();
-    cta_carry.flag = 0;
-    sh[4] = head_pending0 ? 1 : 0;
+    sm.carry.acc = op.identity();
+    sm.carry.flag = 0;
+    sm.carry.pad = 0;
+    sm.head_pending = offsets[I0] < J0 ? 1 : 0;  // list I0 has elements in earlier CTAs
   }
   long long ci = I0, cj = J0, cd = d_begin;
+  long long waited_e = 0, waited_o = 0;      // stages known to be full
+  long long released_e = 0, released_o = 0;  // stages handed back
   bool timed_out = false;
+
+  auto wait_full = [&](uint64_t* bars, int nst, long long stage) {
+    if (timed_out) return;  // after one expired wait, never wait again
+    const int slot = (int)(stage % nst);
+    const uint32_t parity = (uint32_t)((stage / nst) & 1);
+    if (!mbar_wait(&bars[slot], parity, 1u << 22)) timed_out = true;
+  };
+  auto seg = [&](const V& a, const V& bb) -> V {
+    V r;
+    r.flag = a.flag | bb.flag;
+    r.acc = bb.flag ? bb.acc : op.combine(a.acc, bb.acc);
+    r.pad = 0;
+    return r;
+  };
+  V ident;
+  ident.acc = op.identity();
+  ident.flag = 0;
+  ident.pad = 0;
 
   while (cd < d_end) {
     const int len = (int)(d_end - cd < IPC ? d_end - cd : IPC);
-    if (use_tma) {
-      if (!mbar_wait(bar, phase, 1u << 22)) timed_out = true;
-      phase ^= 1;
-    }
-    __syncthreads();
+    // window sizes (clamped at 0 so inconsistent offsets cannot index outside)
     const long long Lrem = I1 - ci;
-    const int Lw = (int)(Lrem < IPC ? Lrem : IPC);
+    const int Lw = (int)(Lrem < 0 ? 0 : (Lrem < IPC ? Lrem : IPC));
     const long long Erem = J1 - cj;
-    const int Ew = (int)(Erem < IPC ? Erem : IPC);
-    const int obase = (int)(ci % RL);
-    const int xbase = (int)(cj % RE);
-    auto A = [&](int k) -> long long {  // end of list ci+k
-      int s = obase + 1 + k;
-      if (s >= RL) s -= RL;
-      return oring[s];
-    };
-    auto S = [&](int k) -> long long {  // start of list ci+k
-      int s = obase + k;
-      if (s >= RL) s -= RL;
-      return oring[s];
-    };
-    // merge-path split of local diagonal dl within the resident windows
-    auto split = [&](int dl) -> int {
-      int lo = dl - Ew > 0 ? dl - Ew : 0;
-      int hi = dl < Lw ? dl : Lw;
+    const int Ew = (int)(Erem < 0 ? 0 : (Erem < IPC ? Erem : IPC));
+    // wait for the stages holding offsets[ci .. ci+Lw] and content[cj .. cj+Ew)
+    const long long need_o = (ci + Lw - OB) / kOStage;
+    while (waited_o <= need_o && waited_o < no_st) wait_full(sm.full_o, kOStages, waited_o++);
+    if (Ew > 0) {
+      const long long need_e = (cj + Ew - 1 - EB) / kEStage;
+      while (waited_e <= need_e && waited_e < ne_st) wait_full(sm.full_e, kEStages, waited_e++);
+    }
+    // linear chunk-local list ends with a sentinel after the window
+    {
+      const int obase = (int)(((ci + 1 - OB) % RO + RO) % RO);
+      for (int kk = tid; kk <= Lw; kk += kConsumers) {
+        int v = kLendBig;
+        if (kk < Lw) {
+          int s = obase + kk;
+          if (s >= RO) s -= RO;
+          const long long rel = sm.oring[s] - cj;
+          v = rel < kLendBig ? (int)rel : kLendBig;
+        }
+        sm.lend[kk] = v;
+      }
+      if (tid == 0) sm.lstart0 = sm.oring[((ci - OB) % RO + RO) % RO] - cj;
+    }
+    consumer_sync();
+    const int xb = (int)((cj - EB) & (long long)(RE - 1));
+    const long long lstart0 = sm.lstart0;
+
+    // this thread's items: local diagonal [dt, dt + nitems)
+    const int dt = tid * IPT;
+    const int nitems = dt < len ? (len - dt < IPT ? len - dt : IPT) : 0;
+    int k = 0;
+    if (nitems) {
+      int lo = dt - Ew > 0 ? dt - Ew : 0;
+      int hi = dt < Lw ? dt : Lw;
       while (lo < hi) {
-        int mid = (lo + hi) >> 1;
-        if ((long long)mid + (A(mid) - cj) < dl) lo = mid + 1;
+        const int mid = (lo + hi) >> 1;
+        if (mid + sm.lend[mid] < dt) lo = mid + 1;
         else hi = mid;
       }
-      return lo;
-    };
-    if (tid == 0) {
-      int kend = split(len);
-      sh[5] = kend;
+      k = lo < Lw ? lo : Lw;
     }
-    const int dt = tid * IPT;
-    int k = dt < len ? split(dt) : 0;
     int m = dt - k;
-    __syncthreads();
-    const int kend = (int)sh[5];
-    const long long ci_next = ci + kend, cj_next = cj + (len - kend);
-
-    // prefetch the next chunk's windows into the slots freed by consumed data
-    const long long ohi_next = (ci_next + IPC < I1 ? ci_next + IPC : I1) + 1;
-    const long long ehi_next = cj_next + IPC < J1 ? cj_next + IPC : J1;
-    if (use_tma) {
-      if (tid == 0) {
-        fence_proxy_async_smem();
-        uint32_t nb = ring_fill<int64_t, RL>(oring, offsets, ohi, ohi_next, bar, true, false) +
-                      ring_fill<Store, RE>(xring, x, ehi, ehi_next, bar, true, false);
-        mbar_arrive_expect_tx(bar, nb);
-        ring_fill<int64_t, RL>(oring, offsets, ohi, ohi_next, bar, true, true);
-        ring_fill<Store, RE>(xring, x, ehi, ehi_next, bar, true, true);
-      }
-    } else {
-      ring_fill_coop<BLOCK, int64_t, RL>(oring, offsets, ohi, ohi_next);
-      ring_fill_coop<BLOCK, Store, RE>(xring, x, ehi, ehi_next);
-    }
-
-    // walk IPT merge items
     Acc acc = op.identity();
     Acc head_acc = op.identity();
     bool has_end = false;
-    long long head_list = -1;
-    const int nitems = dt < len ? (len - dt < IPT ? len - dt : IPT) : 0;
+    int head_k = -1;
     for (int s = 0; s < nitems; s++) {
-      bool take_end = (k < Lw) && (m >= Ew || A(k) <= cj + m);
-      if (take_end) {
-        const long long list = ci + k;
+      if (sm.lend[k] <= m) {
         if (!has_end) {
           has_end = true;
-          head_list = list;
+          head_k = k;
           head_acc = acc;
         } else {
-          out[list] = op.finalize(acc, list);
+          out[ci + k] = op.finalize(acc, ci + k);
         }
         acc = op.identity();
         k++;
       } else {
-        if (m >= Ew) break;  // inconsistent offsets: never read past the window
-        const long long j = cj + m;
-        const Store v = xring[(xbase + m) & (RE - 1)];
+        const Store v = sm.ering[(xb + m) & (RE - 1)];
         bool first = false;
-        if (Op::kNeedsFirst) first = (S(k) == j);
-        acc = op.combine(acc, op.lift(v, j, first, ci + k));
+        if (Op::kNeedsFirst) first = ((long long)m == (k == 0 ? lstart0 : (long long)sm.lend[k - 1]));
+        acc = op.combine(acc, op.lift(v, cj + m, first, ci + k));
         m++;
       }
     }
+    if (nitems && dt + nitems == len) sm.kend = k;  // state after the chunk's last item
 
-    // block segmented scan of the thread tails
-    auto seg = [&](const V& a, const V& bb) -> V {
-      V r;
-      r.flag = a.flag | bb.flag;
-      r.acc = bb.flag ? bb.acc : op.combine(a.acc, bb.acc);
-      r.pad = 0;
-      return r;
-    };
-    V ident;
-    ident.acc = op.identity();
-    ident.flag = 0;
-    ident.pad = 0;
+    // block segmented scan of the thread tails (consumer warps only)
     V mine;
     mine.acc = acc;
     mine.flag = has_end ? 1u : 0u;
     mine.pad = 0;
-    V total;
-    V excl = block_exclusive_scan<BLOCK>(mine, seg, ident, scan_smem, &total);
-    const V carry = cta_carry;
-    V cin = seg(carry, excl);
+    V incl = warp_inclusive_scan(mine, seg, ident);
+    if (lane == 31) sm.scan[warp] = incl;
+    consumer_sync();
+    if (warp == 0) {
+      V w = lane < kConsumers / 32 ? sm.scan[lane] : ident;
+      V wi = warp_inclusive_scan(w, seg, ident);
+      if (lane < kConsumers / 32) sm.scan[lane] = wi;
+    }
+    consumer_sync();
+    V excl = shfl_up(incl, 1);
+    if (lane == 0) excl = ident;
+    if (warp > 0) excl = seg(sm.scan[warp - 1], excl);
+    const V total = sm.scan[kConsumers / 32 - 1];
+    const V carry = sm.carry;
+    const V cin = seg(carry, excl);
     if (has_end) {
-      Acc whole = op.combine(cin.acc, head_acc);
-      if (head_list == I0 && sh[4]) {
-        // list I0 began in an earlier CTA: leave it to the fix-up
-        records[b].head_list = I0;
+      const Acc whole = op.combine(cin.acc, head_acc);
+      const long long list = ci + head_k;
+      if (list == I0 && sm.head_pending) {
+        records[b].head_list = I0;  // began in an earlier CTA: left to the fix-up
         records[b].head_acc = whole;
       } else {
-        out[head_list] = op.finalize(whole, head_list);
+        out[list] = op.finalize(whole, list);
       }
     }
-    __syncthreads();
+    consumer_sync();
+    const int kend = sm.kend;
     if (tid == 0) {
-      cta_carry = seg(carry, total);
-      if (total.flag) sh[4] = 0;
+      sm.carry = seg(carry, total);
+      if (total.flag) sm.head_pending = 0;
     }
-    ci = ci_next;
-    cj = cj_next;
+    ci += kend;
+    cj += len - kend;
     cd += len;
-    ohi = ohi_next;
-    ehi = ehi_next;
-    __syncthreads();
+    // hand fully consumed stages back to the producer
+    while (released_e < waited_e && EB + (released_e + 1) * kEStage <= cj) {
+      if (tid == 0) mbar_arrive(&sm.empty_e[released_e % kEStages]);
+      released_e++;
+    }
+    while (released_o < waited_o && OB + (released_o + 1) * kOStage <= ci) {
+      if (tid == 0) mbar_arrive(&sm.empty_o[released_o % kOStages]);
+      released_o++;
+    }
+    consumer_sync();
   }
   if (tid == 0) {
     records[b].tail_list = I1;
-    records[b].tail_acc = cta_carry.acc;
+    records[b].tail_acc = sm.carry.acc;
     records[b].tail_fresh = (I1 < nlists) ? (offsets[I1] >= J0 ? 1 : 0) : 1;
   }
-  if (timed_out) raise_error(err, inv, GB_MSG_TIMEOUT);
+  // every issued stage completes before the CTA exits
+  while (waited_o < no_st) wait_full(sm.full_o, kOStages, waited_o++);
+  while (waited_e < ne_st) wait_full(sm.full_e, kEStages, waited_e++);
+  if (timed_out && tid == 0) raise_error(err, inv, GB_MSG_TIMEOUT);
 }
 
 // One block: resolve lists that cross CTA boundaries, in CTA order.
@@ -359,8 +441,7 @@ __global__ void __launch_bounds__(BLOCK)
                             typename Op::Out* __restrict__ out,
                             const CtaRecord<typename Op::Acc>* __restrict__ records, int G,
                             int ipc) {
-  using Acc = typename Op::Acc;
-  using V = SegVal<Acc>;
+  using V = SegVal<typename Op::Acc>;
   constexpr int NW = BLOCK / 32;
   __shared__ V scan_smem[NW + 1];
   __shared__ V running;
@@ -385,9 +466,8 @@ __global__ void __launch_bounds__(BLOCK)
   for (int base = 0; base < Geff; base += BLOCK) {
     const int c = base + threadIdx.x;
     V mine = ident;
-    long long tl = -1;
     if (c < Geff) {
-      tl = records[c].tail_list;
+      const long long tl = records[c].tail_list;
       mine.acc = records[c].tail_acc;
       mine.flag = (c == 0 || records[c].tail_fresh || records[c - 1].tail_list != tl) ? 1u : 0u;
     }
@@ -395,11 +475,9 @@ __global__ void __launch_bounds__(BLOCK)
     V excl = block_exclusive_scan<BLOCK>(mine, seg, ident, scan_smem, &total);
     V before = seg(running, excl);  // scan through CTA c-1
     if (c < Geff && c > 0) {
-      long long hl = records[c].head_list;
-      if (hl >= 0 && hl < nlists) {
-        Acc whole = op.combine(before.acc, records[c].head_acc);
-        out[hl] = op.finalize(whole, hl);
-      }
+      const long long hl = records[c].head_list;
+      if (hl >= 0 && hl < nlists)
+        out[hl] = op.finalize(op.combine(before.acc, records[c].head_acc), hl);
     }
     __syncthreads();
     if (threadIdx.x == 0) running = seg(running, total);

@@ -7,7 +7,7 @@ import numpy as np
 import awkward_gb300
 from awkward_gb300 import _abi
 from awkward_gb300._signatures import SIGNATURES
-from awkward_gb300.backend import GB300Backend, kernel_key
+from awkward_gb300.kernel_table import GB300Backend, kernel_key
 
 
 def _header_names():
