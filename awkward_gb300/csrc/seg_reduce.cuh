@@ -63,21 +63,24 @@ struct CtaRecord {
 constexpr int kConsumers = 256;  // consumer threads (8 warps)
 constexpr int kProducerWarp = kConsumers / 32;
 constexpr int kSegThreads = kConsumers + 32;
-constexpr int kSegIPT = 8;
-constexpr int kSegIPC = kConsumers * kSegIPT;  // merge items per chunk
-constexpr int kEStage = 512;                   // elements per content stage
-constexpr int kEStages = 8;                    // content ring: 4096 elements
+constexpr int kSegIPT = 16;
+constexpr int kSegIPC = kConsumers * kSegIPT;  // merge items per chunk (at most)
+constexpr int kEStage = 1024;                  // elements per content stage
+constexpr int kEStages = 6;                    // content ring: 6144 elements
 constexpr int kOStage = 256;                   // offsets per offsets stage
-constexpr int kOStages = 12;                   // offsets ring: 3072 entries
+constexpr int kOStages = 6;                    // offsets ring: 1536 entries
+constexpr int kOWin = 1024;                    // list ends visible to one chunk
 constexpr int kLendBig = 0x7fffffff;
 static_assert(kEStages * kEStage >= kSegIPC + kEStage, "content ring too small");
-static_assert(kOStages * kOStage >= kSegIPC + 1 + kOStage, "offsets ring too small");
+static_assert(kOStages * kOStage >= kOWin + 1 + kOStage, "offsets ring too small");
+static_assert((kEStage & (kEStage - 1)) == 0 && (kOStage & (kOStage - 1)) == 0,
+              "stage sizes are powers of two");
 
 template <class Store, class Acc>
 struct SegSmem {
   int64_t oring[kOStages * kOStage];
   Store ering[kEStages * kEStage];
-  int lend[kSegIPC + 1];  // chunk-local list ends (element position relative to cj)
+  int lend[kOWin + 1];  // chunk-local list ends (element position relative to cj)
   SegVal<Acc> scan[kConsumers / 32 + 1];
   SegVal<Acc> carry;
   uint64_t full_e[kEStages], empty_e[kEStages];
@@ -85,6 +88,7 @@ struct SegSmem {
   long long coords[4];
   long long lstart0;  // start of list ci relative to cj
   int kend;
+  int len;
   int head_pending;
 };
 
@@ -178,6 +182,7 @@ __global__ void __launch_bounds__(kSegThreads)
   constexpr int IPC = kSegIPC, IPT = kSegIPT;
   constexpr int RE = kEStages * kEStage;
   constexpr int RO = kOStages * kOStage;
+  static_assert(kEStage == 1024 && kOStage == 256, "stage shifts below assume these sizes");
 
   extern __shared__ __align__(128) unsigned char smem_raw[];
   Sm& sm = *reinterpret_cast<Sm*>(smem_raw);
@@ -278,15 +283,18 @@ __global__ void __launch_bounds__(kSegThreads)
     sm.head_pending = offsets[I0] < J0 ? 1 : 0;  // list I0 has elements in earlier CTAs
   }
   long long ci = I0, cj = J0, cd = d_begin;
-  long long waited_e = 0, waited_o = 0;      // stages known to be full
-  long long released_e = 0, released_o = 0;  // stages handed back
+  int opos = (int)(I0 - OB);  // ring slot of offsets[ci]
+  int xpos = (int)(J0 - EB);  // ring slot of content[cj]
+  // stage bookkeeping (32-bit, incremental): next stage to wait for / release
+  int we = 0, wo = 0, re_ = 0, ro = 0;
+  const int ne = (int)ne_st, no = (int)no_st;
+  long long rel_e_end = EB + kEStage, rel_o_end = OB + kOStage;
   bool timed_out = false;
 
-  auto wait_full = [&](uint64_t* bars, int nst, long long stage) {
+  auto wait_full = [&](uint64_t* bars, int nst, int stage) {
     if (timed_out) return;  // after one expired wait, never wait again
-    const int slot = (int)(stage % nst);
-    const uint32_t parity = (uint32_t)((stage / nst) & 1);
-    if (!mbar_wait(&bars[slot], parity, 1u << 22)) timed_out = true;
+    const int round = stage / nst;
+    if (!mbar_wait(&bars[stage - round * nst], (uint32_t)(round & 1), 1u << 22)) timed_out = true;
   };
   auto seg = [&](const V& a, const V& bb) -> V {
     V r;
@@ -301,36 +309,39 @@ __global__ void __launch_bounds__(kSegThreads)
   ident.pad = 0;
 
   while (cd < d_end) {
-    const int len = (int)(d_end - cd < IPC ? d_end - cd : IPC);
-    // window sizes (clamped at 0 so inconsistent offsets cannot index outside)
+    // windows (clamped at 0 so inconsistent offsets cannot index outside)
     const long long Lrem = I1 - ci;
-    const int Lw = (int)(Lrem < 0 ? 0 : (Lrem < IPC ? Lrem : IPC));
+    const int La = (int)(Lrem < 0 ? 0 : (Lrem < kOWin ? Lrem : kOWin));
     const long long Erem = J1 - cj;
     const int Ew = (int)(Erem < 0 ? 0 : (Erem < IPC ? Erem : IPC));
-    // wait for the stages holding offsets[ci .. ci+Lw] and content[cj .. cj+Ew)
-    const long long need_o = (ci + Lw - OB) / kOStage;
-    while (waited_o <= need_o && waited_o < no_st) wait_full(sm.full_o, kOStages, waited_o++);
-    if (Ew > 0) {
-      const long long need_e = (cj + Ew - 1 - EB) / kEStage;
-      while (waited_e <= need_e && waited_e < ne_st) wait_full(sm.full_e, kEStages, waited_e++);
+    // wait for the stages holding offsets[ci .. ci+La] and content[cj .. cj+Ew)
+    {
+      const int need_o = (int)((ci + La - OB) >> 8);  // kOStage = 256
+      while (wo <= need_o && wo < no) wait_full(sm.full_o, kOStages, wo++);
+      if (Ew > 0) {
+        const int need_e = (int)((cj + Ew - 1 - EB) >> 10);  // kEStage = 1024
+        while (we <= need_e && we < ne) wait_full(sm.full_e, kEStages, we++);
+      }
     }
     // linear chunk-local list ends with a sentinel after the window
-    {
-      const int obase = (int)(((ci + 1 - OB) % RO + RO) % RO);
-      for (int kk = tid; kk <= Lw; kk += kConsumers) {
-        int v = kLendBig;
-        if (kk < Lw) {
-          int s = obase + kk;
-          if (s >= RO) s -= RO;
-          const long long rel = sm.oring[s] - cj;
-          v = rel < kLendBig ? (int)rel : kLendBig;
-        }
-        sm.lend[kk] = v;
+    for (int kk = tid; kk <= La; kk += kConsumers) {
+      int v = kLendBig;
+      if (kk < La) {
+        int s = opos + 1 + kk;
+        if (s >= RO) s -= RO;
+        const long long rel = sm.oring[s] - cj;
+        v = rel < kLendBig ? (int)rel : kLendBig;
       }
-      if (tid == 0) sm.lstart0 = sm.oring[((ci - OB) % RO + RO) % RO] - cj;
+      sm.lend[kk] = v;
     }
+    if (tid == 0) sm.lstart0 = sm.oring[opos] - cj;
     consumer_sync();
-    const int xb = (int)((cj - EB) & (long long)(RE - 1));
+    // chunk length: at most IPC items, and never past the last visible list end
+    int len = (int)(d_end - cd < IPC ? d_end - cd : IPC);
+    if (La < Lrem && La > 0) {
+      const long long lim = (long long)La + sm.lend[La - 1];
+      if (lim < len) len = (int)(lim > 0 ? lim : 1);
+    }
     const long long lstart0 = sm.lstart0;
 
     // this thread's items: local diagonal [dt, dt + nitems)
@@ -339,13 +350,13 @@ __global__ void __launch_bounds__(kSegThreads)
     int k = 0;
     if (nitems) {
       int lo = dt - Ew > 0 ? dt - Ew : 0;
-      int hi = dt < Lw ? dt : Lw;
+      int hi = dt < La ? dt : La;
       while (lo < hi) {
         const int mid = (lo + hi) >> 1;
         if (mid + sm.lend[mid] < dt) lo = mid + 1;
         else hi = mid;
       }
-      k = lo < Lw ? lo : Lw;
+      k = lo < La ? lo : La;
     }
     int m = dt - k;
     Acc acc = op.identity();
@@ -364,7 +375,9 @@ __global__ void __launch_bounds__(kSegThreads)
         acc = op.identity();
         k++;
       } else {
-        const Store v = sm.ering[(xb + m) & (RE - 1)];
+        int xi = xpos + m;
+        if (xi >= RE) xi -= RE;
+        const Store v = sm.ering[xi];
         bool first = false;
         if (Op::kNeedsFirst) first = ((long long)m == (k == 0 ? lstart0 : (long long)sm.lend[k - 1]));
         acc = op.combine(acc, op.lift(v, cj + m, first, ci + k));
@@ -412,14 +425,20 @@ __global__ void __launch_bounds__(kSegThreads)
     ci += kend;
     cj += len - kend;
     cd += len;
+    opos += kend;
+    if (opos >= RO) opos -= RO;
+    xpos += len - kend;
+    if (xpos >= RE) xpos -= RE;
     // hand fully consumed stages back to the producer
-    while (released_e < waited_e && EB + (released_e + 1) * kEStage <= cj) {
-      if (tid == 0) mbar_arrive(&sm.empty_e[released_e % kEStages]);
-      released_e++;
+    while (re_ < we && rel_e_end <= cj) {
+      if (tid == 0) mbar_arrive(&sm.empty_e[re_ % kEStages]);
+      re_++;
+      rel_e_end += kEStage;
     }
-    while (released_o < waited_o && OB + (released_o + 1) * kOStage <= ci) {
-      if (tid == 0) mbar_arrive(&sm.empty_o[released_o % kOStages]);
-      released_o++;
+    while (ro < wo && rel_o_end <= ci) {
+      if (tid == 0) mbar_arrive(&sm.empty_o[ro % kOStages]);
+      ro++;
+      rel_o_end += kOStage;
     }
     consumer_sync();
   }
@@ -429,8 +448,8 @@ __global__ void __launch_bounds__(kSegThreads)
     records[b].tail_fresh = (I1 < nlists) ? (offsets[I1] >= J0 ? 1 : 0) : 1;
   }
   // every issued stage completes before the CTA exits
-  while (waited_o < no_st) wait_full(sm.full_o, kOStages, waited_o++);
-  while (waited_e < ne_st) wait_full(sm.full_e, kEStages, waited_e++);
+  while (wo < no) wait_full(sm.full_o, kOStages, wo++);
+  while (we < ne) wait_full(sm.full_e, kEStages, we++);
   if (timed_out && tid == 0) raise_error(err, inv, GB_MSG_TIMEOUT);
 }
 
