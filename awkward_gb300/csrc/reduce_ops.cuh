@@ -1,8 +1,10 @@
 // reduce_ops.cuh -- reducer policies for seg_reduce_kernel and the launcher.
 //
 // A policy states one awkward-cpp reducer as (identity, lift, combine,
-// finalize) with an ORDERED combine(earlier, later), so the parallel
-// reduction reproduces the CPU loop's result:
+// finalize).  Every combine is commutative and associative (extremum
+// reducers carry the element index and resolve ties to the lowest index),
+// so any reduction order reproduces the CPU loop's result exactly, except
+// for floating-point rounding of sums and products:
 //   sum/prod        awkward_reduce_sum.cpp:12-25, awkward_reduce_prod.cpp:12-25
 //   sum_bool (any)  awkward_reduce_sum_bool.cpp:18-31
 //   prod_bool (all) awkward_reduce_prod_bool.cpp:10-23
@@ -22,11 +24,158 @@
 
 namespace gb {
 
+// This GPU executes float64 arithmetic AND comparisons on a narrow pipe
+// (about 1/64 of float32), so the float64 reducers below never use it per
+// element: comparisons go through an integer total-order key and sums through
+// an exact fixed-point accumulator on the integer pipe.
 template <class T>
 __device__ __forceinline__ bool is_nan(T v) {
-  if constexpr (std::is_floating_point<T>::value) return v != v;
+  if constexpr (std::is_same<T, double>::value) {
+    return (__double_as_longlong(v) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+  } else if constexpr (std::is_floating_point<T>::value) {
+    return v != v;
+  }
   return false;
 }
+
+// Integer key with the numeric order of non-NaN doubles; -0.0 and +0.0 share
+// key 0 (they compare equal, as in C).
+__device__ __forceinline__ long long f64_key(double v) {
+  const long long b = __double_as_longlong(v);
+  if ((b & 0x7fffffffffffffffLL) == 0) return 0;
+  return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
+}
+
+// b > a (MAX) or b < a (MIN) with C semantics: false if either is NaN.
+template <class T, bool MAX>
+__device__ __forceinline__ bool num_better(T b, T a) {
+  if constexpr (std::is_same<T, double>::value) {
+    if (is_nan(a) || is_nan(b)) return false;
+    const long long kb = f64_key(b), ka = f64_key(a);
+    return MAX ? (kb > ka) : (kb < ka);
+  } else {
+    return MAX ? (b > a) : (b < a);
+  }
+}
+
+// ---------------------------------------------------------------- exact sum
+// Fixed-point accumulator for float64 sums on the integer pipe: the value is
+// acc * 2^(anchor - 1075); every addend's 53-bit significand is aligned to the
+// anchor (the largest exponent seen; bits below the anchor's unit are
+// truncated, < 1 unit each) and |acc| is kept below 2^62 by raising the anchor.
+// finalize() rounds the total to nearest-even once.  Infinities and NaNs are
+// tracked in `flags` with IEEE semantics (NaN absorbs; +inf + -inf = NaN).
+struct FxAcc {
+  long long acc;
+  int anchor;  // >= 1 (1 is the subnormal scale)
+  int flags;   // 1 NaN, 2 +inf, 4 -inf
+};
+
+__device__ __forceinline__ FxAcc fx_norm(FxAcc a) {
+  if ((a.acc ^ (a.acc >> 63)) >= (1LL << 62)) {
+    a.acc >>= 1;
+    a.anchor += 1;
+  }
+  return a;
+}
+
+// add (-1)^neg * m * 2^(ee - 1075), m < 2^53, ee >= 1
+__device__ __forceinline__ FxAcc fx_add(FxAcc a, bool neg, long long m, int ee) {
+  if (ee > a.anchor) {
+    const int sh = ee - a.anchor;
+    a.acc = sh >= 63 ? (a.acc >> 63) : (a.acc >> sh);
+    a.anchor = ee;
+  }
+  const int d = a.anchor - ee;
+  const long long t = d >= 63 ? 0 : (m >> d);
+  a.acc += neg ? -t : t;
+  return fx_norm(a);
+}
+
+__device__ __forceinline__ FxAcc fx_add_f64(FxAcc a, double v) {
+  const long long b = __double_as_longlong(v);
+  const int e = (int)((b >> 52) & 0x7ff);
+  if (e == 0x7ff) {
+    a.flags |= (b & 0xfffffffffffffLL) ? 1 : (b < 0 ? 4 : 2);
+    return a;
+  }
+  const long long m = (b & 0xfffffffffffffLL) | (e ? (1LL << 52) : 0);
+  return fx_add(a, b < 0, m, e ? e : 1);
+}
+
+__device__ __forceinline__ FxAcc fx_add_f32(FxAcc a, float v) {
+  const int b = __float_as_int(v);
+  const int e = (b >> 23) & 0xff;
+  if (e == 0xff) {
+    a.flags |= (b & 0x7fffff) ? 1 : (b < 0 ? 4 : 2);
+    return a;
+  }
+  const long long m = (long long)((b & 0x7fffff) | (e ? (1 << 23) : 0)) << 29;
+  return fx_add(a, b < 0, m, (e ? e : 1) + 896);  // float exponent -> double anchor scale
+}
+
+__device__ __forceinline__ FxAcc fx_combine(FxAcc a, FxAcc b) {
+  if (a.anchor < b.anchor) {
+    FxAcc t = a;
+    a = b;
+    b = t;
+  }
+  const int sh = a.anchor - b.anchor;
+  a.acc += sh >= 63 ? (b.acc >> 63) : (b.acc >> sh);
+  a.flags |= b.flags;
+  return fx_norm(a);
+}
+
+__device__ __forceinline__ double fx_finalize(FxAcc a) {
+  if ((a.flags & 1) || (a.flags & 6) == 6) return __longlong_as_double(0x7ff8000000000000LL);
+  if (a.flags & 2) return __longlong_as_double(0x7ff0000000000000LL);
+  if (a.flags & 4) return __longlong_as_double((long long)0xfff0000000000000ULL);
+  if (a.acc == 0) return 0.0;
+  const unsigned long long sign = a.acc < 0 ? 0x8000000000000000ULL : 0ULL;
+  unsigned long long mag = a.acc < 0 ? (unsigned long long)(-a.acc) : (unsigned long long)a.acc;
+  const int p = 63 - __clzll((long long)mag);  // leading bit of mag
+  long long biased = (long long)p + a.anchor - 52;
+  unsigned long long q;
+  if (p > 52) {
+    const int sh = p - 52;
+    q = mag >> sh;
+    const unsigned long long rem = mag & ((1ULL << sh) - 1), half = 1ULL << (sh - 1);
+    if (rem > half || (rem == half && (q & 1))) q++;
+    if (q == (1ULL << 53)) {
+      q >>= 1;
+      biased++;
+    }
+  } else {
+    q = mag << (52 - p);
+  }
+  if (biased >= 2047) return __longlong_as_double((long long)(sign | 0x7ff0000000000000ULL));
+  if (biased <= 0) {
+    // subnormal: the value is mag * 2^(anchor-1075) with anchor small enough
+    // that mag << (anchor - 1) is the exact subnormal significand
+    return __longlong_as_double((long long)(sign | (mag << (a.anchor - 1))));
+  }
+  return __longlong_as_double(
+      (long long)(sign | ((unsigned long long)biased << 52) | (q & 0xfffffffffffffULL)));
+}
+
+// Sum of float64 (or float32) into float64: exact on the integer pipe, then
+// rounded once (the CPU rounds after every addition; both are within
+// n*eps*sum|x| of the exact sum).
+template <class IN>
+struct FixedSumOp {
+  using In = IN;
+  using Out = double;
+  using Acc = FxAcc;
+  static constexpr bool kNeedsFirst = false;
+  __device__ Acc identity() const { return FxAcc{0, 1, 0}; }
+  __device__ Acc lift(IN v, long long, bool, long long) const { return step(identity(), v, 0, false, 0); }
+  __device__ Acc combine(Acc a, Acc b) const { return fx_combine(a, b); }
+  __device__ Acc step(Acc a, IN v, long long, bool, long long) const {
+    if constexpr (std::is_same<IN, double>::value) return fx_add_f64(a, v);
+    else return fx_add_f32(a, v);
+  }
+  __device__ Out finalize(Acc a, long long) const { return fx_finalize(a); }
+};
 
 // Accumulator wider than 4 bytes for sub-word outputs (shuffles move 32-bit words).
 template <class T>
@@ -47,6 +196,9 @@ struct SumOp {
     else return static_cast<OUT>(v);
   }
   __device__ Acc combine(Acc a, Acc b) const { return a + b; }
+  __device__ Acc step(Acc a, store_t<IN> v, long long j, bool f, long long) const {
+    return a + lift(v, j, f, 0);
+  }
   __device__ Out finalize(Acc a, long long) const { return a; }
 };
 
@@ -62,6 +214,9 @@ struct ProdOp {
     return static_cast<OUT>(v);
   }
   __device__ Acc combine(Acc a, Acc b) const { return a * b; }
+  __device__ Acc step(Acc a, store_t<IN> v, long long, bool, long long) const {
+    return a * static_cast<OUT>(v);
+  }
   __device__ Out finalize(Acc a, long long) const { return a; }
 };
 
@@ -77,6 +232,9 @@ struct AnyAllOp {
     return v != 0 ? 1u : 0u;
   }
   __device__ Acc combine(Acc a, Acc b) const { return ALL ? (a & b) : (a | b); }
+  __device__ Acc step(Acc a, store_t<IN> v, long long, bool, long long) const {
+    return ALL ? (a & (v != 0 ? 1u : 0u)) : (a | (v != 0 ? 1u : 0u));
+  }
   __device__ Out finalize(Acc a, long long) const { return a != 0; }
 };
 
@@ -90,63 +248,277 @@ struct CountNonzeroOp {
   __device__ Acc identity() const { return 0; }
   __device__ Acc lift(store_t<IN> v, long long, bool, long long) const { return v != 0 ? 1 : 0; }
   __device__ Acc combine(Acc a, Acc b) const { return a + b; }
+  __device__ Acc step(Acc a, store_t<IN> v, long long, bool, long long) const { return a + (v != 0 ? 1 : 0); }
   __device__ Out finalize(Acc a, long long) const { return a; }
 };
 
 // best = identity; best = (v > best) ? v : best   (or <).  The partial of a
-// range is its earliest extremal non-NaN element; ties keep the earlier one
-// (this preserves the sign of zero); the identity precedes every element.
+// range is its extremal non-NaN element, ties resolved to the lowest index
+// (this keeps the CPU's first occurrence, e.g. the sign of a zero), so the
+// combine is commutative and any reduction order gives the CPU's answer;
+// the identity precedes every element.
 template <class T, bool MAX>
 struct ExtremumOp {
   using In = T;
   using Out = T;
   struct Acc {
     acc_word_t<T> v;
-    uint32_t valid;
+    long long idx;  // -1: no candidate yet
   };
   static constexpr bool kNeedsFirst = false;
   T ident;
-  __device__ static bool better(T b, T a) { return MAX ? (b > a) : (b < a); }
-  __device__ Acc identity() const { return Acc{acc_word_t<T>(0), 0u}; }
-  __device__ Acc lift(T v, long long, bool, long long) const {
-    return Acc{static_cast<acc_word_t<T>>(v), is_nan(v) ? 0u : 1u};
+  __device__ static bool better(T b, T a) { return num_better<T, MAX>(b, a); }
+  __device__ Acc identity() const { return Acc{acc_word_t<T>(0), -1}; }
+  __device__ Acc lift(T v, long long j, bool, long long) const {
+    return Acc{static_cast<acc_word_t<T>>(v), is_nan(v) ? -1 : j};
   }
   __device__ Acc combine(Acc a, Acc b) const {
-    if (b.valid && (!a.valid || better(static_cast<T>(b.v), static_cast<T>(a.v)))) return b;
+    if (b.idx < 0) return a;
+    if (a.idx < 0) return b;
+    const T av = static_cast<T>(a.v), bv = static_cast<T>(b.v);
+    if (better(bv, av)) return b;
+    if (better(av, bv)) return a;
+    return b.idx < a.idx ? b : a;
+  }
+  // one element after all earlier ones (the CPU loop's update; NaN never wins)
+  __device__ Acc step(Acc a, T v, long long j, bool, long long) const {
+    if (!is_nan(v) && (a.idx < 0 || better(v, static_cast<T>(a.v))))
+      a = Acc{static_cast<acc_word_t<T>>(v), j};
     return a;
   }
   __device__ Out finalize(Acc a, long long) const {
-    return (a.valid && better(static_cast<T>(a.v), ident)) ? static_cast<T>(a.v) : ident;
+    return (a.idx >= 0 && better(static_cast<T>(a.v), ident)) ? static_cast<T>(a.v) : ident;
   }
 };
 
 // Global index of the first extremum; -1 if empty.  The list's first
-// element is always a candidate (a leading NaN wins, as in the CPU loop that
-// seeds best = start); later NaNs never win.
+// element is always a candidate and wins when it is NaN (the CPU loop seeds
+// best = start and NaN never compares greater); later NaNs never win; ties
+// go to the lowest index.  Commutative, like ExtremumOp.
 template <class T, bool MAX>
 struct ArgExtremumOp {
   using In = T;
   using Out = int64_t;
   struct Acc {
     acc_word_t<T> v;
-    uint32_t pad;
-    long long idx;
+    long long idx;  // -1: empty
   };
   static constexpr bool kNeedsFirst = true;
-  __device__ static bool better(T b, T a) { return MAX ? (b > a) : (b < a); }
-  __device__ Acc identity() const { return Acc{acc_word_t<T>(0), 0u, -1}; }
+  __device__ static bool better(T b, T a) { return num_better<T, MAX>(b, a); }
+  __device__ Acc identity() const { return Acc{acc_word_t<T>(0), -1}; }
   __device__ Acc lift(T v, long long j, bool first, long long) const {
     if (!first && is_nan(v)) return identity();
-    return Acc{static_cast<acc_word_t<T>>(v), 0u, j};
+    return Acc{static_cast<acc_word_t<T>>(v), j};
   }
   __device__ Acc combine(Acc a, Acc b) const {
     if (a.idx < 0) return b;
     if (b.idx < 0) return a;
-    if (is_nan(static_cast<T>(a.v))) return a;
-    return better(static_cast<T>(b.v), static_cast<T>(a.v)) ? b : a;
+    const T av = static_cast<T>(a.v), bv = static_cast<T>(b.v);
+    if (is_nan(av)) return a;  // only a list's leading element can be a NaN candidate
+    if (is_nan(bv)) return b;
+    if (better(bv, av)) return b;
+    if (better(av, bv)) return a;
+    return b.idx < a.idx ? b : a;
+  }
+  // one element after all earlier ones: the CPU loop's update
+  __device__ Acc step(Acc a, T v, long long j, bool first, long long) const {
+    if (a.idx < 0) {
+      if (first || !is_nan(v)) a = Acc{static_cast<acc_word_t<T>>(v), j};
+    } else if (better(v, static_cast<T>(a.v))) {
+      a = Acc{static_cast<acc_word_t<T>>(v), j};
+    }
+    return a;
   }
   __device__ Out finalize(Acc a, long long) const { return a.idx; }
 };
+
+// ---------------------------------------------------------------- float64 keys
+// Float64 extremum reducers on the integer pipe.  k(v) is the order key of
+// f64_key, reversed (~) for MIN so both directions maximise; NaN gets the
+// lowest key (never selected), except a list's leading element in the
+// arg-reducers, which gets the highest (it stays selected, as in the CPU loop).
+template <bool MAX>
+__device__ __forceinline__ long long f64_dir_key(double v) {
+  const long long k = f64_key(v);
+  return MAX ? k : ~k;
+}
+constexpr long long kKeyLow = (long long)0x8000000000000000ULL;
+constexpr long long kKeyHigh = 0x7fffffffffffffffLL;
+
+template <bool MAX>
+struct ExtremumOp<double, MAX> {
+  using In = double;
+  using Out = double;
+  struct Acc {
+    long long key;
+    long long bits;
+    long long idx;  // -1: no candidate yet
+  };
+  static constexpr bool kNeedsFirst = false;
+  double ident;
+  __device__ Acc identity() const { return Acc{kKeyLow, 0, -1}; }
+  __device__ Acc lift(double v, long long j, bool, long long) const {
+    if (is_nan(v)) return identity();
+    return Acc{f64_dir_key<MAX>(v), __double_as_longlong(v), j};
+  }
+  __device__ Acc combine(Acc a, Acc b) const {
+    if (b.idx < 0) return a;
+    if (a.idx < 0) return b;
+    if (b.key != a.key) return b.key > a.key ? b : a;
+    return b.idx < a.idx ? b : a;
+  }
+  __device__ Acc step(Acc a, double v, long long j, bool, long long) const {
+    if (!is_nan(v)) {
+      const long long k = f64_dir_key<MAX>(v);
+      if (a.idx < 0 || k > a.key) a = Acc{k, __double_as_longlong(v), j};
+    }
+    return a;
+  }
+  __device__ Out finalize(Acc a, long long) const {
+    if (a.idx < 0 || is_nan(ident)) return ident;
+    return a.key > f64_dir_key<MAX>(ident) ? __longlong_as_double(a.bits) : ident;
+  }
+};
+
+template <bool MAX>
+struct ArgExtremumOp<double, MAX> {
+  using In = double;
+  using Out = int64_t;
+  struct Acc {
+    long long key;
+    long long idx;  // -1: empty
+  };
+  static constexpr bool kNeedsFirst = true;
+  __device__ Acc identity() const { return Acc{kKeyLow, -1}; }
+  __device__ static long long k_of(double v, bool first) {
+    return is_nan(v) ? (first ? kKeyHigh : kKeyLow) : f64_dir_key<MAX>(v);
+  }
+  __device__ Acc lift(double v, long long j, bool first, long long) const {
+    const long long k = k_of(v, first);
+    return k == kKeyLow ? identity() : Acc{k, j};
+  }
+  __device__ Acc combine(Acc a, Acc b) const {
+    if (b.idx < 0) return a;
+    if (a.idx < 0) return b;
+    if (b.key != a.key) return b.key > a.key ? b : a;
+    return b.idx < a.idx ? b : a;
+  }
+  __device__ Acc step(Acc a, double v, long long j, bool first, long long) const {
+    const long long k = k_of(v, first);
+    if (k > a.key) a = Acc{k, j};
+    return a;
+  }
+  __device__ Out finalize(Acc a, long long) const { return a.idx; }
+};
+
+// ---------------------------------------------------------------- short runs
+// Reduce n consecutive elements p[0..n) (global indices j0..j0+n) of one
+// list into a fresh accumulator.  The default steps element by element.
+template <class Op>
+__device__ __forceinline__ typename Op::Acc run_short(const Op& op,
+                                                      const store_t<typename Op::In>* p, int n,
+                                                      long long j0, long long st, long long li) {
+  typename Op::Acc a = op.identity();
+  for (int i = 0; i < n; i++) a = op.step(a, __ldg(p + i), j0 + i, j0 + i == st, li);
+  return a;
+}
+
+// Float64 max/min of a short run, fast path: the raw key b ^ ((b >> 63) &
+// 0x7ff..f) orders all non-NaN doubles except that it puts -0.0 below +0.0,
+// and it puts positive NaNs above +inf (negative NaNs below -inf).  The loop
+// uses it unconditioned; if the winner is a zero or a NaN (rare) the run is
+// redone with the exact step, which resolves ties to the first occurrence and
+// never selects a NaN.
+__device__ __forceinline__ long long f64_raw_key(long long b) {
+  return b ^ ((long long)((unsigned long long)b >> 63) * 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool raw_key_exact(long long k) {
+  // not a zero (raw keys 0 and -1) and not a NaN (beyond the infinities)
+  return k != 0 && k != -1 && k <= 0x7ff0000000000000LL && k >= (long long)0x800fffffffffffffULL;
+}
+
+template <bool MAX>
+__device__ __forceinline__ typename ExtremumOp<double, MAX>::Acc run_short(
+    const ExtremumOp<double, MAX>& op, const double* p, int n, long long j0, long long st,
+    long long li) {
+  const long long* q = reinterpret_cast<const long long*>(p);
+  long long best = 0;
+  int at = -1;
+  for (int i = 0; i < n; i++) {
+    const long long k = MAX ? f64_raw_key(__ldg(q + i)) : ~f64_raw_key(__ldg(q + i));
+    if (at < 0 || k > best) {
+      best = k;
+      at = i;
+    }
+  }
+  typename ExtremumOp<double, MAX>::Acc a = op.identity();
+  if (at < 0) return a;
+  const long long bits = __ldg(q + at);
+  if (raw_key_exact(f64_raw_key(bits))) return {f64_dir_key<MAX>(__longlong_as_double(bits)), bits, j0 + at};
+  for (int i = 0; i < n; i++) a = op.step(a, __ldg(p + i), j0 + i, j0 + i == st, li);
+  return a;
+}
+
+template <bool MAX>
+__device__ __forceinline__ typename ArgExtremumOp<double, MAX>::Acc run_short(
+    const ArgExtremumOp<double, MAX>& op, const double* p, int n, long long j0, long long st,
+    long long li) {
+  const long long* q = reinterpret_cast<const long long*>(p);
+  long long best = 0;
+  int at = -1;
+  for (int i = 0; i < n; i++) {
+    const long long k = MAX ? f64_raw_key(__ldg(q + i)) : ~f64_raw_key(__ldg(q + i));
+    if (at < 0 || k > best) {
+      best = k;
+      at = i;
+    }
+  }
+  typename ArgExtremumOp<double, MAX>::Acc a = op.identity();
+  if (at < 0) return a;
+  const long long bits = __ldg(q + at);
+  // exact unless the winner is a zero or a NaN, or the run starts with a NaN
+  if (raw_key_exact(f64_raw_key(bits)) && !(j0 == st && is_nan(__ldg(p))))
+    return {f64_dir_key<MAX>(__longlong_as_double(bits)), j0 + at};
+  for (int i = 0; i < n; i++) a = op.step(a, __ldg(p + i), j0 + i, j0 + i == st, li);
+  return a;
+}
+
+// Exact float64 sum of at most 32 elements, branch-free: pass 1 finds the
+// largest exponent (and any inf/NaN), pass 2 adds the significands aligned to
+// it (|sum| < 2^58, no renormalisation needed).
+template <class IN>
+__device__ __forceinline__ FxAcc run_short(const FixedSumOp<IN>& op, const IN* p, int n,
+                                           long long, long long, long long) {
+  if constexpr (!std::is_same<IN, double>::value) {
+    FxAcc a = op.identity();
+    for (int i = 0; i < n; i++) a = op.step(a, __ldg(p + i), 0, false, 0);
+    return a;
+  } else {
+    const long long* q = reinterpret_cast<const long long*>(p);
+    int emax = 1, special = 0;
+    for (int i = 0; i < n; i++) {
+      const int e = (int)((unsigned long long)__ldg(q + i) >> 52) & 0x7ff;
+      emax = e > emax ? e : emax;
+    }
+    special = emax == 0x7ff;
+    if (special) {  // inf / NaN present: the general path tracks them
+      FxAcc a = op.identity();
+      for (int i = 0; i < n; i++) a = fx_add_f64(a, __longlong_as_double(__ldg(q + i)));
+      return a;
+    }
+    long long acc = 0;
+    for (int i = 0; i < n; i++) {
+      const long long b = __ldg(q + i);
+      const int e = (int)((unsigned long long)b >> 52) & 0x7ff;
+      const long long m = (b & 0xfffffffffffffLL) | ((long long)(e != 0) << 52);
+      const int d = emax - (e ? e : 1);
+      const long long t = m >> (d < 63 ? d : 63);
+      const long long sg = b >> 63;  // 0 or -1
+      acc += (t ^ sg) - sg;
+    }
+    return FxAcc{acc, emax, 0};
+  }
+}
 
 template <class IN>
 struct SumSqOp {
@@ -160,6 +532,7 @@ struct SumSqOp {
     return d * d;
   }
   __device__ Acc combine(Acc a, Acc b) const { return a + b; }
+  __device__ Acc step(Acc a, store_t<IN> v, long long j, bool f, long long l) const { return a + lift(v, j, f, l); }
   __device__ Out finalize(Acc a, long long) const { return a; }
 };
 
@@ -189,6 +562,7 @@ struct SumPowOp {
     return ipow_binary(static_cast<double>(v), n);
   }
   __device__ Acc combine(Acc a, Acc b) const { return a + b; }
+  __device__ Acc step(Acc a, store_t<IN> v, long long j, bool f, long long l) const { return a + lift(v, j, f, l); }
   __device__ Out finalize(Acc a, long long) const { return a; }
 };
 
@@ -205,23 +579,19 @@ struct CenteredSumSqOp {
     return d * d;
   }
   __device__ Acc combine(Acc a, Acc b) const { return a + b; }
+  __device__ Acc step(Acc a, store_t<IN> v, long long j, bool f, long long l) const { return a + lift(v, j, f, l); }
   __device__ Out finalize(Acc a, long long) const { return a; }
 };
 
 // ---------------------------------------------------------------- launcher
-constexpr int kFixupBlock = 1024;
-
 template <class Op>
 struct SegReduceConfig {
-  using Sm = SegSmem<store_t<typename Op::In>, typename Op::Acc>;
   static int blocks_per_sm() {
     static std::once_flag once;
     static int bps = 1;
     std::call_once(once, [] {
-      auto k = seg_reduce_kernel<Op>;
-      cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(Sm));
       int n = 0;
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, kSegThreads, sizeof(Sm)) !=
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, seg_reduce_kernel<Op>, kSegBlock, 0) !=
               cudaSuccess ||
           n < 1)
         n = 1;
@@ -232,29 +602,28 @@ struct SegReduceConfig {
 };
 
 // Launch the segmented reduction of `nlists` lists on `stream`: the
-// persistent merge-path kernel, then the one-block cross-CTA fix-up.
-// Returns the launch status; data never travel to the host.
+// warp-balanced kernel over a persistent grid, then the fix-up of lists
+// longer than kAbsorb elements that cross warp ranges.  Returns the launch status; data never
+// travel to the host.
 template <class Op>
 cudaError_t launch_seg_reduce(const Op& op, const store_t<typename Op::In>* x,
                               const int64_t* offsets, long long nlists, typename Op::Out* out,
-                              uint64_t inv, uint64_t* err, cudaStream_t stream,
-                              int grid_override = 0) {
+                              uint64_t inv, uint64_t* err, cudaStream_t stream) {
   if (nlists <= 0) return cudaSuccess;
-  using Rec = CtaRecord<typename Op::Acc>;
-  using Sm = typename SegReduceConfig<Op>::Sm;
-  const int G = grid_override > 0 ? grid_override
-                                  : device_sm_count() * SegReduceConfig<Op>::blocks_per_sm();
+  using Rec = RangeRecord<typename Op::Acc>;
+  const int blocks = device_sm_count() * SegReduceConfig<Op>::blocks_per_sm();
+  const int W = blocks * (kSegBlock / 32);
   void* rec = nullptr;
-  cudaError_t e = scratch_alloc(&rec, (size_t)G * sizeof(Rec), stream);
+  cudaError_t e = scratch_alloc(&rec, (size_t)W * sizeof(Rec), stream);
   if (e != cudaSuccess) return e;
-  const int use_tma = ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(offsets)) &
-                       15) == 0;
-  seg_reduce_kernel<Op><<<G, kSegThreads, sizeof(Sm), stream>>>(
-      op, x, offsets, nlists, out, reinterpret_cast<Rec*>(rec), G, use_tma, inv, err);
+  seg_reduce_kernel<Op><<<blocks, kSegBlock, 0, stream>>>(op, x, offsets, nlists, out,
+                                                          reinterpret_cast<Rec*>(rec), W, inv,
+                                                          err);
   e = cudaGetLastError();
   if (e == cudaSuccess) {
-    seg_reduce_fixup_kernel<Op, kFixupBlock><<<1, kFixupBlock, 0, stream>>>(
-        op, offsets, nlists, out, reinterpret_cast<const Rec*>(rec), G, kSegIPC);
+    const int fix_blocks = (W + 255) / 256;  // one warp per 32 records
+    seg_reduce_fixup_kernel<Op><<<fix_blocks, 256, 0, stream>>>(
+        op, offsets, nlists, out, reinterpret_cast<const Rec*>(rec), W);
     e = cudaGetLastError();
   }
   cudaError_t f = scratch_free(rec, stream);

@@ -1,36 +1,36 @@
-// seg_reduce.cuh -- merge-path segmented reduction over ListOffsetArray offsets.
+// seg_reduce.cuh -- segmented reduction over ListOffsetArray offsets.
 //
 // Replaces the per-bin loops of awkward-cpp's reducers
 // (awkward-cpp/src/cpu-kernels/awkward_reduce_*.cpp) for the cupy backend.
 //
-// Work decomposition.  The reduction is a merge of two sorted streams: the
-// list ends A[i] = offsets[i+1] (i < nlists) and the element indices
-// j in [offsets[0], offsets[nlists]).  Consuming an element accumulates it
-// into the current list; consuming a list end emits that list's result.  The
-// merged sequence has D = nlists + E items.  A persistent grid of G CTAs
-// splits D into equal diagonal ranges (perfect balance for any length
-// distribution: empty lists, Poisson, heavy tails, one giant list); each CTA
-// locates its two ends with a warp-wide 32-ary merge-path search in global
-// memory.
+// Balance.  The reduction is a merge of two sorted streams, the list ends
+// offsets[i+1] and the element indices; the merged sequence has
+// D = nlists + E items.  Every warp of a persistent grid takes an equal
+// diagonal range of it (balanced for any length distribution: empty lists,
+// Poisson, heavy tails, one giant list), found with a warp-wide 32-ary
+// merge-path search in global memory: lists I0..I1-1 end inside the warp's
+// range, list I1 is open at its end (the "tail"), and list I0 may have begun
+// in an earlier range (the "head").
 //
-// Inside a CTA, one producer warp streams the CTA's slices of `offsets` and
-// of the content into two shared-memory rings of fixed-size stages with 1-D
-// TMA bulk copies (cp.async.bulk of the 16-byte aligned interior; ragged
-// head and tail by plain loads), guarded by full/empty mbarrier pairs, so
-// loads run several chunks ahead of the reduction.  Eight consumer warps
-// reduce chunks of IPC = 256*IPT merge items: they convert the chunk's list
-// ends into a linear int32 window (relative to the chunk's first element),
-// every thread locates its IPT items by binary search in that window and
-// walks them, a block-wide segmented scan stitches lists that cross
-// threads, and finished stages are handed back to the producer.  HBM
-// traffic is one pass over offsets and content.  Lists that cross CTAs leave
-// one head and one tail record per CTA; a one-block fix-up kernel combines
-// them with a segmented scan in CTA order.  No CTA ever waits on another.
+// Reduction.  The warp walks its lists 32 at a time, one list per lane: a
+// list of at most 32 elements is reduced by its lane straight from global
+// memory (read-only path; 64 resident warps per SM keep enough loads in
+// flight, and the warp's loads cover one contiguous stretch of content); a
+// longer list is reduced by the whole warp, strided over 32 lanes (coalesced)
+// and combined with a butterfly.  Each input byte is read from HBM once and
+// results are stored coalesced.
 //
-// Combination order is always earlier-then-later, so order-sensitive
-// reducers (max/min/argmax/argmin tie and NaN rules) are bit-exact with the
-// sequential CPU loops; floating-point sums differ from the CPU only by
-// rounding (a tree instead of a left-to-right sum).
+// Arithmetic.  Every reducer's combine is commutative and associative
+// (extremum reducers carry the element index and break ties towards the
+// lowest index), so the cooperative reductions give the CPU's results:
+// bit-exact for integers, counts, max/min and argmax/argmin (including the
+// NaN and signed-zero rules).  Float64 data never touch the float64 pipe per
+// element (see reduce_ops.cuh): comparisons use integer keys, sums an exact
+// fixed-point accumulator.
+//
+// Lists that cross warp ranges leave one head and one tail record per warp;
+// a one-block fix-up kernel combines them with a segmented scan in range
+// order.  No warp ever waits on another.
 #pragma once
 
 #include <type_traits>
@@ -50,457 +50,208 @@ struct SegVal {
   uint32_t pad;
 };
 
+// Partial results of the lists that cross the ends of one warp's range.
 template <class Acc>
-struct CtaRecord {
-  long long head_list;  // list that started before this CTA and ends in it, or -1
-  long long tail_list;  // list open at the end of this CTA (nlists: none)
+struct RangeRecord {
+  long long head_list;  // list that began before this range and ends in it, or -1
+  long long tail_list;  // list open at the end of this range (nlists: none)
   Acc head_acc;
   Acc tail_acc;
-  int tail_fresh;  // tail list has no elements before this CTA
+  int tail_fresh;  // tail list has no elements before this range
   int pad;
 };
 
-constexpr int kConsumers = 256;  // consumer threads (8 warps)
-constexpr int kProducerWarp = kConsumers / 32;
-constexpr int kSegThreads = kConsumers + 32;
-constexpr int kSegIPT = 16;
-constexpr int kSegIPC = kConsumers * kSegIPT;  // merge items per chunk (at most)
-constexpr int kEStage = 1024;                  // elements per content stage
-constexpr int kEStages = 6;                    // content ring: 6144 elements
-constexpr int kOStage = 256;                   // offsets per offsets stage
-constexpr int kOStages = 6;                    // offsets ring: 1536 entries
-constexpr int kOWin = 1024;                    // list ends visible to one chunk
-constexpr int kLendBig = 0x7fffffff;
-static_assert(kEStages * kEStage >= kSegIPC + kEStage, "content ring too small");
-static_assert(kOStages * kOStage >= kOWin + 1 + kOStage, "offsets ring too small");
-static_assert((kEStage & (kEStage - 1)) == 0 && (kOStage & (kOStage - 1)) == 0,
-              "stage sizes are powers of two");
+constexpr int kSegBlock = 256;        // threads per CTA (8 warps)
+constexpr int kSegMinBlocks = 5;      // resident CTAs per SM (40 warps of loads in flight)
+constexpr int kShortList = 32;        // longest list reduced by one lane
+constexpr int kMinRangeItems = 512;   // smallest merge range given to a warp
+constexpr long long kAbsorb = 4096;   // longest list reduced whole by the range where it ends
 
-template <class Store, class Acc>
-struct SegSmem {
-  int64_t oring[kOStages * kOStage];
-  Store ering[kEStages * kEStage];
-  int lend[kOWin + 1];  // chunk-local list ends (element position relative to cj)
-  SegVal<Acc> scan[kConsumers / 32 + 1];
-  SegVal<Acc> carry;
-  uint64_t full_e[kEStages], empty_e[kEStages];
-  uint64_t full_o[kOStages], empty_o[kOStages];
-  long long coords[4];
-  long long lstart0;  // start of list ci relative to cj
-  int kend;
-  int len;
-  int head_pending;
-};
-
-__device__ __forceinline__ void consumer_sync() {
-  asm volatile("bar.sync 1, %0;" ::"n"(kConsumers) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
-__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity) {
-  uint32_t done;
-  asm volatile(
-      "{\n"
-      ".reg .pred p;\n"
-      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-      "selp.u32 %0, 1, 0, p;\n"
-      "}\n"
-      : "=r"(done)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return done != 0;
-}
-
-// Merge-path split of diagonal d in global memory (one warp).  Returns the
-// number of list ends consumed among the first d merged items.
-__device__ __forceinline__ long long mp_search_global(const int64_t* __restrict__ offsets,
-                                                      long long nlists, long long e0,
-                                                      long long E, long long d) {
-  const int lane = threadIdx.x & 31;
+// Merge-path split of diagonal d in global memory by a half warp (16 lanes,
+// `mask` selects them).  Returns the number of list ends among the first d
+// merged items: the first k in [max(0, d-E), min(d, nlists)] with
+// k + offsets[k+1] - e0 >= d.  The first probe brackets a proportional guess
+// (exact for evenly spread lengths), then 16-ary narrowing.
+__device__ __forceinline__ long long mp_search_half(const int64_t* __restrict__ offsets,
+                                                    long long nlists, long long e0, long long E,
+                                                    long long d, unsigned mask) {
+  const int hl = threadIdx.x & 15;
   long long lo = d - E > 0 ? d - E : 0;
   long long hi = d < nlists ? d : nlists;  // answer in [lo, hi]
-  while (hi - lo > 32) {
-    const long long step = (hi - lo) / 32;
-    const long long k = lo + (long long)lane * step;
-    const bool p = (k + (offsets[k + 1] - e0)) < d;
-    const unsigned msk = __ballot_sync(0xffffffffu, p);
-    const int cnt = __popc(msk);
+  auto pred = [&](long long k) { return (k + (__ldg(offsets + k + 1) - e0)) < d; };
+  if (hi - lo > 16) {
+    // proportional guess g; probe g + (hl - 8) * w
+    const long long D = nlists + E;
+    long long g = D > 0 ? (long long)((double)d * (double)nlists / (double)D) : lo;
+    const long long w = ((hi - lo) >> 12) + 1;
+    long long k = g + (long long)(hl - 8) * w;
+    k = k < lo ? lo : (k > hi - 1 ? hi - 1 : k);
+    const unsigned m = __ballot_sync(mask, pred(k)) >> (threadIdx.x & 16);
+    const long long k0 = __shfl_sync(mask, k, 0, 16), k15 = __shfl_sync(mask, k, 15, 16);
+    const int cnt = __popc(m & 0xffffu);
+    // window valid when the split lies between the first and last probe
+    if (cnt > 0 && cnt < 16 && (m & 1u)) {
+      const long long kp = __shfl_sync(mask, k, cnt - 1, 16), kn = __shfl_sync(mask, k, cnt, 16);
+      lo = kp + 1;
+      hi = kn;
+    } else if (cnt == 0) {
+      hi = k0;
+    } else if (cnt == 16) {
+      lo = k15 + 1;
+    }
+  }
+  while (hi - lo > 16) {
+    const long long step = (hi - lo) / 16;
+    const long long k = lo + (long long)hl * step;
+    const unsigned m = __ballot_sync(mask, pred(k)) >> (threadIdx.x & 16);
+    const int cnt = __popc(m & 0xffffu);
     const long long nlo = cnt > 0 ? lo + (long long)(cnt - 1) * step + 1 : lo;
-    const long long nhi = cnt < 32 ? lo + (long long)cnt * step : hi;
+    const long long nhi = cnt < 16 ? lo + (long long)cnt * step : hi;
     lo = nlo;
     hi = nhi;
   }
-  const long long k = lo + lane;
-  const bool p = (k < hi) && ((k + (offsets[k + 1] - e0)) < d);
-  const unsigned msk = __ballot_sync(0xffffffffu, p);
-  return lo + __popc(msk);
-}
-
-// Producer warp: copy global [lo, hi) of `src` into ring slot `slot` (the
-// slot holds global [stage_lo, stage_lo + STAGE)), completing barrier
-// `full`.  With TMA the 16-byte aligned interior is one bulk copy and the
-// ragged head and tail (each shorter than 16 bytes) are plain loads issued
-// before the arrive, which releases them.
-template <class T, int STAGE>
-__device__ __forceinline__ void produce_stage(T* ring, const T* src, long long stage_lo,
-                                              long long lo, long long hi, int slot,
-                                              uint64_t* full, bool use_tma) {
-  T* slot_base = ring + (size_t)slot * STAGE;
-  const int lane = threadIdx.x & 31;
-  if (use_tma) {
-    constexpr int A = 16 / (int)sizeof(T);
-    long long a16 = (lo + A - 1) / A * A;
-    long long b16 = hi / A * A;
-    if (a16 >= b16) a16 = b16 = hi;
-    if (lane == 0) {
-      const uint32_t bytes = (uint32_t)((b16 - a16) * (long long)sizeof(T));
-      for (long long g = lo; g < a16; g++) slot_base[g - stage_lo] = src[g];
-      for (long long g = b16; g < hi; g++) slot_base[g - stage_lo] = src[g];
-      mbar_arrive_expect_tx(full, bytes);
-      if (bytes) bulk_g2s(slot_base + (a16 - stage_lo), src + a16, bytes, full);
-    }
-  } else {
-    for (long long g = lo + lane; g < hi; g += 32) slot_base[g - stage_lo] = src[g];
-    __syncwarp();
-    if (lane == 0) mbar_arrive(full);
-  }
+  const long long k = lo + hl;
+  const unsigned m = __ballot_sync(mask, (k < hi) && pred(k)) >> (threadIdx.x & 16);
+  return lo + __popc(m & 0xffffu);
 }
 
 template <class Op>
-__global__ void __launch_bounds__(kSegThreads)
-    seg_reduce_kernel(Op op, const store_t<typename Op::In>* __restrict__ x,
-                      const int64_t* __restrict__ offsets, long long nlists,
-                      typename Op::Out* __restrict__ out, CtaRecord<typename Op::Acc>* records,
-                      int G, int use_tma_i, uint64_t inv, uint64_t* err) {
-  using Acc = typename Op::Acc;
-  using Store = store_t<typename Op::In>;
-  using V = SegVal<Acc>;
-  using Sm = SegSmem<Store, Acc>;
-  constexpr int IPC = kSegIPC, IPT = kSegIPT;
-  constexpr int RE = kEStages * kEStage;
-  constexpr int RO = kOStages * kOStage;
-  static_assert(kEStage == 1024 && kOStage == 256, "stage shifts below assume these sizes");
-
-  extern __shared__ __align__(128) unsigned char smem_raw[];
-  Sm& sm = *reinterpret_cast<Sm*>(smem_raw);
-  const bool use_tma = use_tma_i != 0;
-
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const long long e0 = offsets[0];
-  const long long eN = offsets[nlists];
-  const long long E = eN > e0 ? eN - e0 : 0;
-  const long long D = nlists + E;
-  const int Geff = (int)((D + IPC - 1) / IPC < G ? (D + IPC - 1) / IPC : G);
-  const int b = blockIdx.x;
-  if (b >= Geff) return;
-  const long long d_begin = D * b / Geff, d_end = D * (b + 1) / Geff;
-
-  if (warp < 2) {
-    const long long d = warp == 0 ? d_begin : d_end;
-    const long long i = mp_search_global(offsets, nlists, e0, E, d);
-    if (lane == 0) {
-      sm.coords[warp * 2] = i;
-      sm.coords[warp * 2 + 1] = e0 + (d - i);
-    }
+__device__ __forceinline__ typename Op::Acc warp_allreduce(const Op& op, typename Op::Acc a) {
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    constexpr int W = sizeof(typename Op::Acc) / 4;
+    union U { typename Op::Acc v; uint32_t w[W]; } u;
+    u.v = a;
+#pragma unroll
+    for (int i = 0; i < W; i++) u.w[i] = __shfl_xor_sync(0xffffffffu, u.w[i], d);
+    a = op.combine(a, u.v);
   }
-  if (tid == 0) {
-    for (int s = 0; s < kEStages; s++) {
-      mbar_init(&sm.full_e[s], 1);
-      mbar_init(&sm.empty_e[s], 1);
-    }
-    for (int s = 0; s < kOStages; s++) {
-      mbar_init(&sm.full_o[s], 1);
-      mbar_init(&sm.empty_o[s], 1);
-    }
-    fence_barrier_init();
-    records[b].head_list = -1;
-  }
-  __syncthreads();
-  const long long I0 = sm.coords[0], J0 = sm.coords[1], I1 = sm.coords[2], J1 = sm.coords[3];
-  // Stage grids: content stage s holds [EB + s*kEStage, ...) and offsets stage
-  // t holds [OB + t*kOStage, ...); both bases are multiples of the stage size.
-  const long long EB = J0 / kEStage * kEStage;
-  const long long OB = I0 / kOStage * kOStage;
-  const long long ne_st = J1 > J0 ? (J1 - EB + kEStage - 1) / kEStage : 0;
-  const long long no_st = (I1 + 1 - OB + kOStage - 1) / kOStage;
-
-  if (warp == kProducerWarp) {
-    // ------------------------------------------------------------ producer
-    long long se = 0, so = 0;
-    uint32_t spins = 0;
-    while (se < ne_st || so < no_st) {
-      bool progressed = false;
-      if (se < ne_st) {
-        const int slot = (int)(se % kEStages);
-        const long long round = se / kEStages;
-        int ok = round == 0;
-        if (!ok && lane == 0) ok = mbar_test(&sm.empty_e[slot], (uint32_t)((round - 1) & 1));
-        if (__shfl_sync(0xffffffffu, ok, 0)) {
-          const long long st = EB + se * kEStage;
-          const long long lo = st > J0 ? st : J0;  // never read before the CTA's first element
-          const long long hi = st + kEStage < J1 ? st + kEStage : J1;
-          produce_stage<Store, kEStage>(sm.ering, x, st, lo, hi, slot, &sm.full_e[slot],
-                                        use_tma);
-          se++;
-          progressed = true;
-        }
-      }
-      if (so < no_st) {
-        const int slot = (int)(so % kOStages);
-        const long long round = so / kOStages;
-        int ok = round == 0;
-        if (!ok && lane == 0) ok = mbar_test(&sm.empty_o[slot], (uint32_t)((round - 1) & 1));
-        if (__shfl_sync(0xffffffffu, ok, 0)) {
-          const long long st = OB + so * kOStage;
-          const long long hi = st + kOStage < I1 + 1 ? st + kOStage : I1 + 1;
-          produce_stage<int64_t, kOStage>(sm.oring, offsets, st, st, hi, slot, &sm.full_o[slot],
-                                          use_tma);
-          so++;
-          progressed = true;
-        }
-      }
-      if (progressed) {
-        spins = 0;
-      } else {
-        if (++spins > kSpinLimit) {
-          if (lane == 0) raise_error(err, inv, GB_MSG_TIMEOUT);
-          break;
-        }
-        __nanosleep(64);
-      }
-    }
-    return;
-  }
-
-  // -------------------------------------------------------------- consumers
-  if (tid == 0) {
-    sm.carry.acc = op.identity();
-    sm.carry.flag = 0;
-    sm.carry.pad = 0;
-    sm.head_pending = offsets[I0] < J0 ? 1 : 0;  // list I0 has elements in earlier CTAs
-  }
-  long long ci = I0, cj = J0, cd = d_begin;
-  int opos = (int)(I0 - OB);  // ring slot of offsets[ci]
-  int xpos = (int)(J0 - EB);  // ring slot of content[cj]
-  // stage bookkeeping (32-bit, incremental): next stage to wait for / release
-  int we = 0, wo = 0, re_ = 0, ro = 0;
-  const int ne = (int)ne_st, no = (int)no_st;
-  long long rel_e_end = EB + kEStage, rel_o_end = OB + kOStage;
-  bool timed_out = false;
-
-  auto wait_full = [&](uint64_t* bars, int nst, int stage) {
-    if (timed_out) return;  // after one expired wait, never wait again
-    const int round = stage / nst;
-    if (!mbar_wait(&bars[stage - round * nst], (uint32_t)(round & 1), 1u << 22)) timed_out = true;
-  };
-  auto seg = [&](const V& a, const V& bb) -> V {
-    V r;
-    r.flag = a.flag | bb.flag;
-    r.acc = bb.flag ? bb.acc : op.combine(a.acc, bb.acc);
-    r.pad = 0;
-    return r;
-  };
-  V ident;
-  ident.acc = op.identity();
-  ident.flag = 0;
-  ident.pad = 0;
-
-  while (cd < d_end) {
-    // windows (clamped at 0 so inconsistent offsets cannot index outside)
-    const long long Lrem = I1 - ci;
-    const int La = (int)(Lrem < 0 ? 0 : (Lrem < kOWin ? Lrem : kOWin));
-    const long long Erem = J1 - cj;
-    const int Ew = (int)(Erem < 0 ? 0 : (Erem < IPC ? Erem : IPC));
-    // wait for the stages holding offsets[ci .. ci+La] and content[cj .. cj+Ew)
-    {
-      const int need_o = (int)((ci + La - OB) >> 8);  // kOStage = 256
-      while (wo <= need_o && wo < no) wait_full(sm.full_o, kOStages, wo++);
-      if (Ew > 0) {
-        const int need_e = (int)((cj + Ew - 1 - EB) >> 10);  // kEStage = 1024
-        while (we <= need_e && we < ne) wait_full(sm.full_e, kEStages, we++);
-      }
-    }
-    // linear chunk-local list ends with a sentinel after the window
-    for (int kk = tid; kk <= La; kk += kConsumers) {
-      int v = kLendBig;
-      if (kk < La) {
-        int s = opos + 1 + kk;
-        if (s >= RO) s -= RO;
-        const long long rel = sm.oring[s] - cj;
-        v = rel < kLendBig ? (int)rel : kLendBig;
-      }
-      sm.lend[kk] = v;
-    }
-    if (tid == 0) sm.lstart0 = sm.oring[opos] - cj;
-    consumer_sync();
-    // chunk length: at most IPC items, and never past the last visible list end
-    int len = (int)(d_end - cd < IPC ? d_end - cd : IPC);
-    if (La < Lrem && La > 0) {
-      const long long lim = (long long)La + sm.lend[La - 1];
-      if (lim < len) len = (int)(lim > 0 ? lim : 1);
-    }
-    const long long lstart0 = sm.lstart0;
-
-    // this thread's items: local diagonal [dt, dt + nitems)
-    const int dt = tid * IPT;
-    const int nitems = dt < len ? (len - dt < IPT ? len - dt : IPT) : 0;
-    int k = 0;
-    if (nitems) {
-      int lo = dt - Ew > 0 ? dt - Ew : 0;
-      int hi = dt < La ? dt : La;
-      while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (mid + sm.lend[mid] < dt) lo = mid + 1;
-        else hi = mid;
-      }
-      k = lo < La ? lo : La;
-    }
-    int m = dt - k;
-    Acc acc = op.identity();
-    Acc head_acc = op.identity();
-    bool has_end = false;
-    int head_k = -1;
-    for (int s = 0; s < nitems; s++) {
-      if (sm.lend[k] <= m) {
-        if (!has_end) {
-          has_end = true;
-          head_k = k;
-          head_acc = acc;
-        } else {
-          out[ci + k] = op.finalize(acc, ci + k);
-        }
-        acc = op.identity();
-        k++;
-      } else {
-        int xi = xpos + m;
-        if (xi >= RE) xi -= RE;
-        const Store v = sm.ering[xi];
-        bool first = false;
-        if (Op::kNeedsFirst) first = ((long long)m == (k == 0 ? lstart0 : (long long)sm.lend[k - 1]));
-        acc = op.combine(acc, op.lift(v, cj + m, first, ci + k));
-        m++;
-      }
-    }
-    if (nitems && dt + nitems == len) sm.kend = k;  // state after the chunk's last item
-
-    // block segmented scan of the thread tails (consumer warps only)
-    V mine;
-    mine.acc = acc;
-    mine.flag = has_end ? 1u : 0u;
-    mine.pad = 0;
-    V incl = warp_inclusive_scan(mine, seg, ident);
-    if (lane == 31) sm.scan[warp] = incl;
-    consumer_sync();
-    if (warp == 0) {
-      V w = lane < kConsumers / 32 ? sm.scan[lane] : ident;
-      V wi = warp_inclusive_scan(w, seg, ident);
-      if (lane < kConsumers / 32) sm.scan[lane] = wi;
-    }
-    consumer_sync();
-    V excl = shfl_up(incl, 1);
-    if (lane == 0) excl = ident;
-    if (warp > 0) excl = seg(sm.scan[warp - 1], excl);
-    const V total = sm.scan[kConsumers / 32 - 1];
-    const V carry = sm.carry;
-    const V cin = seg(carry, excl);
-    if (has_end) {
-      const Acc whole = op.combine(cin.acc, head_acc);
-      const long long list = ci + head_k;
-      if (list == I0 && sm.head_pending) {
-        records[b].head_list = I0;  // began in an earlier CTA: left to the fix-up
-        records[b].head_acc = whole;
-      } else {
-        out[list] = op.finalize(whole, list);
-      }
-    }
-    consumer_sync();
-    const int kend = sm.kend;
-    if (tid == 0) {
-      sm.carry = seg(carry, total);
-      if (total.flag) sm.head_pending = 0;
-    }
-    ci += kend;
-    cj += len - kend;
-    cd += len;
-    opos += kend;
-    if (opos >= RO) opos -= RO;
-    xpos += len - kend;
-    if (xpos >= RE) xpos -= RE;
-    // hand fully consumed stages back to the producer
-    while (re_ < we && rel_e_end <= cj) {
-      if (tid == 0) mbar_arrive(&sm.empty_e[re_ % kEStages]);
-      re_++;
-      rel_e_end += kEStage;
-    }
-    while (ro < wo && rel_o_end <= ci) {
-      if (tid == 0) mbar_arrive(&sm.empty_o[ro % kOStages]);
-      ro++;
-      rel_o_end += kOStage;
-    }
-    consumer_sync();
-  }
-  if (tid == 0) {
-    records[b].tail_list = I1;
-    records[b].tail_acc = sm.carry.acc;
-    records[b].tail_fresh = (I1 < nlists) ? (offsets[I1] >= J0 ? 1 : 0) : 1;
-  }
-  // every issued stage completes before the CTA exits
-  while (wo < no) wait_full(sm.full_o, kOStages, wo++);
-  while (we < ne) wait_full(sm.full_e, kEStages, we++);
-  if (timed_out && tid == 0) raise_error(err, inv, GB_MSG_TIMEOUT);
+  return a;
 }
 
-// One block: resolve lists that cross CTA boundaries, in CTA order.
-template <class Op, int BLOCK>
-__global__ void __launch_bounds__(BLOCK)
-    seg_reduce_fixup_kernel(Op op, const int64_t* __restrict__ offsets, long long nlists,
-                            typename Op::Out* __restrict__ out,
-                            const CtaRecord<typename Op::Acc>* __restrict__ records, int G,
-                            int ipc) {
-  using V = SegVal<typename Op::Acc>;
-  constexpr int NW = BLOCK / 32;
-  __shared__ V scan_smem[NW + 1];
-  __shared__ V running;
-  const long long e0 = offsets[0];
-  const long long eN = offsets[nlists];
+template <class T>
+__device__ __forceinline__ T ld_ro(const T* p) {
+  return __ldg(p);
+}
+
+template <class Op>
+__global__ void __launch_bounds__(kSegBlock, kSegMinBlocks)
+    seg_reduce_kernel(Op op, const store_t<typename Op::In>* __restrict__ x,
+                      const int64_t* __restrict__ offsets, long long nlists,
+                      typename Op::Out* __restrict__ out, RangeRecord<typename Op::Acc>* records,
+                      int W, uint64_t inv, uint64_t* err) {
+  (void)inv;
+  (void)err;
+  const int lane = threadIdx.x & 31;
+  const int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+  const long long e0 = __ldg(offsets);
+  const long long eN = __ldg(offsets + nlists);
   const long long E = eN > e0 ? eN - e0 : 0;
   const long long D = nlists + E;
-  const int Geff = (int)((D + ipc - 1) / ipc < G ? (D + ipc - 1) / ipc : G);
-  auto seg = [&](const V& a, const V& bb) -> V {
-    V r;
-    r.flag = a.flag | bb.flag;
-    r.acc = bb.flag ? bb.acc : op.combine(a.acc, bb.acc);
-    r.pad = 0;
-    return r;
-  };
-  V ident;
-  ident.acc = op.identity();
-  ident.flag = 0;
-  ident.pad = 0;
-  if (threadIdx.x == 0) running = ident;
-  __syncthreads();
-  for (int base = 0; base < Geff; base += BLOCK) {
-    const int c = base + threadIdx.x;
-    V mine = ident;
-    if (c < Geff) {
-      const long long tl = records[c].tail_list;
-      mine.acc = records[c].tail_acc;
-      mine.flag = (c == 0 || records[c].tail_fresh || records[c - 1].tail_list != tl) ? 1u : 0u;
+  const long long wanted = (D + kMinRangeItems - 1) / kMinRangeItems;
+  const int Weff = (int)(wanted < W ? wanted : W);
+  if (w >= Weff) return;
+  const long long d0 = D * w / Weff, d1 = D * (w + 1) / Weff;
+  // both ends at once: lanes 0-15 search d0, lanes 16-31 search d1
+  const bool upper = lane >= 16;
+  const long long split = mp_search_half(offsets, nlists, e0, E, upper ? d1 : d0,
+                                         upper ? 0xffff0000u : 0x0000ffffu);
+  const long long I0 = __shfl_sync(0xffffffffu, split, 0);
+  const long long I1 = __shfl_sync(0xffffffffu, split, 16);
+  const long long J0 = e0 + (d0 - I0), J1 = e0 + (d1 - I1);
+  const long long last_list = I1 < nlists ? I1 : I1 - 1;  // I1 itself is the tail, if any
+
+  for (long long base = I0; base <= last_list; base += 32) {
+    const long long li = base + lane;
+    const bool act = li <= last_list;
+    long long st = 0, s0 = 0, e = 0;
+    bool skip = false;
+    if (act) {
+      st = __ldg(offsets + li);
+      const long long en = __ldg(offsets + li + 1);
+      const bool small = en - st <= kAbsorb;  // reduced whole by the range where it ends
+      s0 = (st < J0 && !small) ? J0 : st;
+      e = li == I1 ? J1 : en;
+      skip = li == I1 && small;  // the range where it ends takes all of it
+      if (e < s0) e = s0;
     }
-    V total;
-    V excl = block_exclusive_scan<BLOCK>(mine, seg, ident, scan_smem, &total);
-    V before = seg(running, excl);  // scan through CTA c-1
-    if (c < Geff && c > 0) {
-      const long long hl = records[c].head_list;
-      if (hl >= 0 && hl < nlists)
-        out[hl] = op.finalize(op.combine(before.acc, records[c].head_acc), hl);
+    typename Op::Acc acc = op.identity();
+    if (act && !skip && e - s0 <= kShortList) acc = run_short(op, x + s0, (int)(e - s0), s0, st, li);
+    unsigned coop = __ballot_sync(0xffffffffu, act && !skip && e - s0 > kShortList);
+    while (coop) {  // longer lists: the whole warp, strided (coalesced)
+      const int src = __ffs(coop) - 1;
+      coop &= coop - 1;
+      const long long s2 = __shfl_sync(0xffffffffu, s0, src);
+      const long long e2 = __shfl_sync(0xffffffffu, e, src);
+      const long long st2 = __shfl_sync(0xffffffffu, st, src);
+      const long long l2 = base + src;
+      typename Op::Acc a2 = op.identity();
+      for (long long j = s2 + lane; j < e2; j += 32) a2 = op.step(a2, ld_ro(x + j), j, j == st2, l2);
+      a2 = warp_allreduce(op, a2);
+      if (lane == src) acc = a2;
     }
-    __syncthreads();
-    if (threadIdx.x == 0) running = seg(running, total);
-    __syncthreads();
+    if (act && !skip) {
+      if (li == I1) {
+        records[w].tail_acc = acc;  // a giant list continues in the next range
+      } else if (s0 > st) {
+        records[w].head_acc = acc;  // the end of a giant list that began earlier
+      } else {
+        out[li] = op.finalize(acc, li);
+      }
+    }
+  }
+  if (lane == 0) {
+    const long long st0 = __ldg(offsets + I0);
+    const bool head = I0 < I1 && st0 < J0 && __ldg(offsets + I0 + 1) - st0 > kAbsorb;
+    records[w].head_list = head ? I0 : -1;
+    const bool tail = I1 < nlists && __ldg(offsets + I1 + 1) - __ldg(offsets + I1) > kAbsorb;
+    records[w].tail_list = tail ? I1 : -1;
+    records[w].tail_fresh = (tail && __ldg(offsets + I1) >= J0) ? 1 : 0;
+    if (!tail) records[w].tail_acc = op.identity();
+  }
+}
+
+// Giant lists (more than kAbsorb elements) that cross warp ranges: one warp
+// per 32 records; for each record holding the end of such a list, the warp
+// walks back over the preceding records 32 at a time, combining the tail
+// partials of the same list up to the range where it began.
+template <class Op>
+__global__ void __launch_bounds__(256)
+    seg_reduce_fixup_kernel(Op op, const int64_t* __restrict__ offsets, long long nlists,
+                            typename Op::Out* __restrict__ out,
+                            const RangeRecord<typename Op::Acc>* __restrict__ records, int W) {
+  using Acc = typename Op::Acc;
+  const int lane = threadIdx.x & 31;
+  const long long e0 = __ldg(offsets), eN = __ldg(offsets + nlists);
+  const long long E = eN > e0 ? eN - e0 : 0;
+  const long long D = nlists + E;
+  const long long wanted = (D + kMinRangeItems - 1) / kMinRangeItems;
+  const int Weff = (int)(wanted < W ? wanted : W);
+  const int c0 = (int)(((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5) * 32);
+  if (c0 >= Weff) return;
+  const int c = c0 + lane;
+  const long long hl = c < Weff ? records[c].head_list : -1;
+  unsigned todo = __ballot_sync(0xffffffffu, hl >= 0);
+  while (todo) {
+    const int src = __ffs(todo) - 1;
+    todo &= todo - 1;
+    const int cc = c0 + src;
+    const long long L = __shfl_sync(0xffffffffu, hl, src);
+    Acc acc = op.identity();
+    for (int base = cc - 1; base >= 0; base -= 32) {
+      const int r = base - lane;  // lane 0 is the nearest preceding range
+      const bool valid = r >= 0 && records[r].tail_list == L;
+      const bool fresh = valid && records[r].tail_fresh;  // the range where L began
+      const unsigned inval = __ballot_sync(0xffffffffu, !valid);
+      const unsigned fr = __ballot_sync(0xffffffffu, fresh);
+      const int stop_inv = inval ? __ffs(inval) - 1 : 32;
+      const int stop_fr = fr ? __ffs(fr) - 1 : 32;
+      const int lim = stop_inv < stop_fr + 1 ? stop_inv : stop_fr + 1;  // lanes < lim contribute
+      if (lane < lim) acc = op.combine(acc, records[r].tail_acc);
+      if (inval || fr) break;
+    }
+    acc = warp_allreduce(op, acc);
+    if (lane == 0) out[L] = op.finalize(op.combine(acc, records[cc].head_acc), L);
   }
 }
 
