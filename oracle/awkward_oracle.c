@@ -17,7 +17,7 @@
  *     has them (fixtures in tests/golden/kernel_test_data_subset.json);
  *   - outputs of awkward-cpp's own CPU kernels, compiled from the reference
  *     sources by oracle/build.py, on seeded random inputs
- *     (tests/golden/ref_random_*.npz).
+ *     (tests/golden/ref_random.npz).
  *
  * A pthread driver at the end (oracle_parallel_reduce) splits a reduction
  * over list ranges for the multi-core CPU baseline.
