@@ -11,6 +11,8 @@
 //
 // Error codes are the indices of the messages in awkward's CUDA kernels of
 // the same name (their `// message:` enum order).
+#include <mutex>
+
 #include "list_tile.cuh"
 
 using namespace gb;
@@ -523,3 +525,84 @@ GB_EXPORT int awkward_RegularArray_getitem_jagged_expand_64(int64_t* multistarts
 GB_LOCALINDEX(awkward_ListArray32_localindex_64, int32_t)
 GB_LOCALINDEX(awkward_ListArrayU32_localindex_64, uint32_t)
 GB_LOCALINDEX(awkward_ListArray64_localindex_64, int64_t)
+
+// ================================================================== no-alloc variant
+// A copy of awkward_ListArray64_getitem_jagged_apply_64 for callers that may
+// not allocate device memory at call time.  Such callers are, for example,
+// awkward code embedded in a process whose device memory is owned by another
+// framework's pooling allocator (XLA-style preallocation of most of the GPU,
+// an RMM pool): there cudaMalloc either fails for lack of memory or bypasses
+// the pool's accounting, and the embedded code holds no handle to the pool.
+//
+// The only scratch the kernel needs is the look-back tile states (one
+// 64-bit ticket counter plus one 64-bit word per tile of 1024 lists).  Here
+// they live in a file-scope device array of fixed size, so every GPU that
+// loads the library holds kNoAllocTileWords * 8 bytes (512 KiB + 8 B) until
+// the process exits.  The array is shared by all calls:
+//   * sliceouterlen is limited to kNoAllocMaxLists = 65536 * 1024 lists;
+//     larger calls return cudaErrorInvalidValue without launching anything;
+//   * each call zeroes the words it uses (cudaMemsetAsync on its stream)
+//     before the kernel, because the array keeps the previous call's states;
+//   * two calls whose work overlaps on the GPU (different streams, or
+//     different host threads on one device) race on the array and give wrong
+//     offsets: issue them on one stream or order them with events.
+// The array's host-side name is only a stand-in symbol, not a device
+// address, so the device address is looked up with cudaGetSymbolAddress the
+// first time the entry point runs on each device (with that device current)
+// and cached.  That first call per device should therefore come before any
+// stream capture on that device.  The entry point calls no cudaMalloc,
+// cudaFree or other allocating routine.
+namespace {
+
+constexpr long long kNoAllocMaxTiles = 1ll << 16;
+constexpr long long kNoAllocMaxLists = kNoAllocMaxTiles * kTileLists;
+constexpr long long kNoAllocTileWords = kNoAllocMaxTiles + 1;  // + the ticket counter
+
+static __device__ __align__(256) unsigned long long g_noalloc_tiles[kNoAllocTileWords];
+
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+unsigned long long* g_noalloc_addr[kNoAllocMaxDevices] = {};
+
+// Device address of g_noalloc_tiles on the current device (looked up once).
+cudaError_t noalloc_tiles_address(unsigned long long** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_addr[dev]) {
+    void* ptr = nullptr;
+    e = cudaGetSymbolAddress(&ptr, g_noalloc_tiles);
+    if (e != cudaSuccess) return e;
+    if (!ptr) return cudaErrorInvalidSymbol;
+    g_noalloc_addr[dev] = static_cast<unsigned long long*>(ptr);
+  }
+  *out = g_noalloc_addr[dev];
+  return cudaSuccess;
+}
+
+}  // namespace
+
+GB_EXPORT int awkward_ListArray64_getitem_jagged_apply_64_noalloc(
+    int64_t* tooffsets, int64_t* tocarry, const int64_t* slicestarts, const int64_t* slicestops,
+    int64_t sliceouterlen, const int64_t* sliceindex, int64_t sliceinnerlen,
+    const int64_t* fromstarts, const int64_t* fromstops, int64_t contentlen,
+    uint64_t invocation_index, uint64_t* err_code, void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (sliceouterlen > kNoAllocMaxLists) return (int)cudaErrorInvalidValue;
+  unsigned long long* tiles = nullptr;
+  cudaError_t e = noalloc_tiles_address(&tiles);
+  if (e != cudaSuccess) return (int)e;
+  if (sliceouterlen <= 0) return (int)cudaMemsetAsync(tooffsets, 0, sizeof(int64_t), s);
+  const long long nt = tile_count(sliceouterlen);
+  e = cudaMemsetAsync(tiles, 0, (size_t)(nt + 1) * sizeof(unsigned long long), s);
+  if (e != cudaSuccess) return (int)e;
+  ScanTiles st;
+  st.ticket = tiles;
+  st.status = tiles + 1;
+  jagged_apply_kernel<int64_t><<<(unsigned)nt, kTileBlock, 0, s>>>(
+      tooffsets, tocarry, slicestarts, slicestops, sliceouterlen, sliceindex, sliceinnerlen,
+      fromstarts, fromstops, contentlen, st, invocation_index, err_code);
+  return (int)cudaGetLastError();
+}

@@ -10,6 +10,10 @@ from awkward_gb300._signatures import SIGNATURES
 from awkward_gb300.kernel_table import GB300Backend, kernel_key
 
 
+# The one entry point without a kernel-specification.yml counterpart.
+EXTRA = {"awkward_ListArray64_getitem_jagged_apply_64_noalloc"}
+
+
 def _header_names():
     import os
 
@@ -19,7 +23,7 @@ def _header_names():
 
 
 def test_header_matches_signature_table():
-    assert sorted(_header_names()) == sorted(SIGNATURES)
+    assert sorted(_header_names()) == sorted(set(SIGNATURES) | EXTRA)
 
 
 def test_library_builds_loads_and_exports_every_declaration():
