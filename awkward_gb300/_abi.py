@@ -71,6 +71,24 @@ def cfunc(name):
     return f
 
 
+_EXT_CTYPES = {"int64_t": ctypes.c_int64, "uint64_t": ctypes.c_uint64, "int32_t": ctypes.c_int32}
+
+
+def ext_cfunc(name):
+    """The typed ctypes function of one extension entry point (_extensions.py)."""
+    from ._extensions import EXTENSIONS
+
+    f = _funcs.get(name)
+    if f is None:
+        lib = load_library()
+        f = getattr(lib, name)
+        args, _group = EXTENSIONS[name]
+        f.argtypes = [ctypes.c_void_p if t.endswith("*") else _EXT_CTYPES[t] for t, _a in args]
+        f.restype = ctypes.c_int
+        _funcs[name] = f
+    return f
+
+
 def exported_symbols():
     """Names declared in include/awkward_gb300.h that the loaded library exports."""
     lib = load_library()

@@ -1,0 +1,100 @@
+"""Entry points of libawkward_gb300 that have no kernel-specification.yml counterpart.
+
+One table serves the header generator (gen_signatures.py), the ctypes loader
+(_abi.py) and the export test.  Each entry: name -> (C argument list as
+(type, name) pairs, comment for the header).  All return int (cudaError_t).
+"""
+
+from __future__ import annotations
+
+_NOALLOC_COMMENT = """no-alloc variant.  No counterpart in awkward: an extra entry point
+of this library for callers that may not allocate device memory while
+they run, e.g. code embedded in a process whose GPU memory is owned by
+another framework's pooling allocator (cudaMalloc then fails or goes
+around the pool, and the caller has no handle to the pool).
+Same arguments and results as awkward_ListArray64_getitem_jagged_apply_64;
+its tile-state scratch is a fixed 512 KiB device array inside the
+library (held on every GPU that loads it until exit) instead of a
+pool allocation.  sliceouterlen above AWKWARD_GB300_NOALLOC_MAX_LISTS
+returns cudaErrorInvalidValue (1) and launches nothing.  All calls
+share the array: calls that overlap on the GPU (other streams or
+threads) race and must be ordered by the caller.  The first call on
+each device looks up the array's device address, so make it before
+any stream capture on that device."""
+
+_AUTOGRAD_COMMENT = """backward kernels of differentiable jagged operations (torch.autograd
+in awkward_gb300/autograd.py).  No counterpart in awkward, which has no
+CUDA backward kernels.  Pointers are device pointers; offsets are int64
+[nlists + 1] (need not start at 0); element arrays are indexed globally.
+  segment_sum_backward:   grad_x[j] = grad_out[list of j]
+  segment_max_backward:   grad_x = 0; grad_x[argmax[l]] = grad_out[l] for
+                          argmax[l] in [0, nelements) (global indices, -1 empty)
+  jagged_softmax_forward: y = exp(x - max) / sum(exp(x - max)) per list
+  jagged_softmax_backward: grad_x = y * (grad_y - sum(grad_y * y)) per list,
+                          y from y_saved, or recomputed from x when NULL"""
+
+EXTENSIONS = {
+    "awkward_ListArray64_getitem_jagged_apply_64_noalloc": (
+        [("int64_t*", "tooffsets"), ("int64_t*", "tocarry"), ("const int64_t*", "slicestarts"),
+         ("const int64_t*", "slicestops"), ("int64_t", "sliceouterlen"),
+         ("const int64_t*", "sliceindex"), ("int64_t", "sliceinnerlen"),
+         ("const int64_t*", "fromstarts"), ("const int64_t*", "fromstops"),
+         ("int64_t", "contentlen"), ("uint64_t", "invocation_index"), ("uint64_t*", "err_code"),
+         ("void*", "stream")],
+        "noalloc"),
+}
+
+for _suffix, _t in (("float32", "float"), ("float64", "double")):
+    EXTENSIONS[f"awkward_gb300_segment_sum_backward_{_suffix}"] = (
+        [(f"{_t}*", "grad_x"), (f"const {_t}*", "grad_out"), ("const int64_t*", "offsets"),
+         ("int64_t", "nlists"), ("void*", "stream")], "autograd")
+    EXTENSIONS[f"awkward_gb300_segment_max_backward_{_suffix}"] = (
+        [(f"{_t}*", "grad_x"), (f"const {_t}*", "grad_out"), ("const int64_t*", "argmax"),
+         ("int64_t", "nelements"), ("int64_t", "nlists"), ("void*", "stream")], "autograd")
+    EXTENSIONS[f"awkward_gb300_jagged_softmax_forward_{_suffix}"] = (
+        [(f"{_t}*", "y"), (f"const {_t}*", "x"), ("const int64_t*", "offsets"),
+         ("int64_t", "nlists"), ("void*", "stream")], "autograd")
+    EXTENSIONS[f"awkward_gb300_jagged_softmax_backward_{_suffix}"] = (
+        [(f"{_t}*", "grad_x"), (f"const {_t}*", "grad_y"), (f"const {_t}*", "x"),
+         (f"const {_t}*", "y_saved"), ("const int64_t*", "offsets"), ("int64_t", "nlists"),
+         ("void*", "stream")], "autograd")
+
+_JAGGED_COMMENT = """jagged getitem steps that awkward performs with cupy array operations
+instead of kernels of its specification (no counterpart in
+kernel-specification.yml):
+  jagged_mask_to_index: jagged boolean mask (uint8, one byte per element,
+    indexed globally over offsets[0]..offsets[nlists]) -> new offsets
+    [nlists + 1] and, for each true entry in order, its position within its
+    list (src/awkward/_slicing.py:476-530: localindex + compaction + cumsum);
+  take: out[i] = content[carry[i]] for itemsize 1, 2, 4 or 8 bytes
+    (NumpyArray._carry); a carry outside [0, contentlen) sets err_code to
+    invocation_index*256 + 0 ("index out of range")."""
+
+EXTENSIONS["awkward_gb300_jagged_mask_to_index"] = (
+    [("int64_t*", "tooffsets"), ("int64_t*", "toindex"), ("const uint8_t*", "mask"),
+     ("const int64_t*", "offsets"), ("int64_t", "nlists"), ("uint64_t*", "err_code"),
+     ("void*", "stream")], "jagged")
+EXTENSIONS["awkward_gb300_take"] = (
+    [("void*", "out"), ("const void*", "content"), ("int64_t", "itemsize"),
+     ("const int64_t*", "carry"), ("int64_t", "n"), ("int64_t", "contentlen"),
+     ("uint64_t", "invocation_index"), ("uint64_t*", "err_code"), ("void*", "stream")], "jagged")
+
+GROUP_COMMENTS = {"noalloc": _NOALLOC_COMMENT, "autograd": _AUTOGRAD_COMMENT,
+                  "jagged": _JAGGED_COMMENT}
+GROUP_DEFINES = {"noalloc": ["#define AWKWARD_GB300_NOALLOC_MAX_LISTS 67108864LL"]}
+
+
+def header_lines():
+    """Declarations of the extension entry points, grouped, for the C header."""
+    out = []
+    for group in ("noalloc", "jagged", "autograd"):
+        out.append("")
+        text = GROUP_COMMENTS[group].splitlines()
+        out.append(f"/* ---- {text[0]}")
+        out.extend(f" * {t}".rstrip() for t in text[1:])
+        out[-1] = out[-1] + " */"
+        out.extend(GROUP_DEFINES.get(group, []))
+        for name, (args, g) in EXTENSIONS.items():
+            if g == group:
+                out.append(f"int {name}({', '.join(f'{t} {a}' for t, a in args)});")
+    return out

@@ -6,14 +6,15 @@
 //
 // The CPU enumerates each list's tuples depth-first in lexicographic order.
 // Here every output slot is produced independently: a list tile scans the
-// per-list tuple counts (decoupled look-back), then consecutive threads take
-// consecutive output slots, find their list by binary search and unrank the
-// slot's lexicographic rank into the tuple (combinatorial number system:
-// choose each position by binary search over "tuples whose next element is
-// below v" = C(s-lo, rem) - C(s-v, rem)).  With replacement the
-// non-decreasing tuple over s elements is the strictly increasing tuple over
-// s+n-1 elements with position p shifted down by p.  All n output arrays are
-// written coalesced.
+// per-list tuple counts (decoupled look-back), then each warp fills a
+// contiguous share of the tile's slots, 32 consecutive slots per step; a lane
+// finds its list by walking forward from the list of the step's first slot
+// and unranks the slot's lexicographic rank into the tuple (combinatorial
+// number system: closed forms for n = 1, 2, 3; for larger n each position by
+// bisection over "tuples whose next element is below v" = C(s-lo, rem) -
+// C(s-v, rem)).  With replacement the non-decreasing tuple over s elements is
+// the strictly increasing tuple over s+n-1 elements with position p shifted
+// down by p.  All n output arrays are written coalesced.
 #include "list_tile.cuh"
 
 using namespace gb;
@@ -26,6 +27,7 @@ constexpr int kMaxPtrs = 32;
 __device__ __forceinline__ long long combinations_count(long long size, long long n,
                                                         bool replacement) {
   if (replacement) size += n - 1;
+  if (n == 2 && size < (1ll << 31)) return size < 2 ? 0 : size * (size - 1) / 2;  // same value
   long long thisn = n;
   if (thisn > size) return 0;
   if (thisn == size) return 1;
@@ -74,6 +76,56 @@ __global__ void __launch_bounds__(kTileBlock)
   if (tile == ntiles - 1 && threadIdx.x == 0) totallen[0] = prefix + sm.total;
 }
 
+// Pairs before first element i in a list of s: T(i) = i * (2s - i - 1) / 2.
+__device__ __forceinline__ long long pairs_before(long long s, long long i) {
+  return i * (2 * s - i - 1) / 2;
+}
+
+// Rank -> (i, j), i < j < s, in lexicographic order.  The first element is
+// estimated from the closed form of T(i) <= rank in float32 and corrected
+// exactly with 64-bit integers (a few steps at most for s < 2^20; a bisection
+// above that).
+__device__ __forceinline__ void unrank2(long long s, long long rank, long long* i, long long* j) {
+  long long a;
+  if (s < (1ll << 20)) {
+    const float d = (float)(2 * s - 1);
+    const float disc = fmaxf(d * d - 8.0f * (float)rank, 0.0f);
+    a = (long long)floorf((d - sqrtf(disc)) * 0.5f);
+    a = a < 0 ? 0 : (a > s - 2 ? s - 2 : a);
+    while (a > 0 && pairs_before(s, a) > rank) a--;
+    while (a < s - 2 && pairs_before(s, a + 1) <= rank) a++;
+  } else {
+    long long lo = 0, hi = s - 2;
+    while (lo < hi) {
+      const long long mid = (lo + hi + 1) >> 1;
+      if (pairs_before(s, mid) <= rank) lo = mid;
+      else hi = mid - 1;
+    }
+    a = lo;
+  }
+  *i = a;
+  *j = a + 1 + (rank - pairs_before(s, a));
+}
+
+// The same for lists shorter than 2^15 in 32-bit arithmetic (every product
+// stays below 2^31): float estimate from 1/sqrt, then exact correction.
+__device__ __forceinline__ void unrank2_small(int s, int rank, int* i, int* j) {
+  const float d = (float)(2 * s - 1);
+  const float disc = fmaxf(d * d - 8.0f * (float)rank, 1.0f);
+  int a = (int)((d - disc * rsqrtf(disc)) * 0.5f);
+  a = a < 0 ? 0 : (a > s - 2 ? s - 2 : a);
+  const int two_s1 = 2 * s - 1;
+  while (a > 0 && ((a * (two_s1 - a)) >> 1) > rank) a--;
+  while (a < s - 2 && (((a + 1) * (two_s1 - a - 1)) >> 1) <= rank) a++;
+  *i = a;
+  *j = a + 1 + (rank - ((a * (two_s1 - a)) >> 1));
+}
+
+// C(m, 3) without division in the loop (valid for m < 2^21).
+__device__ __forceinline__ long long binom3(long long m) {
+  return m < 3 ? 0 : m * (m - 1) * (m - 2) / 6;
+}
+
 template <class C>
 __global__ void __launch_bounds__(kTileBlock)
     combinations_kernel(int64_t** __restrict__ tocarry, int64_t* __restrict__ toindex,
@@ -107,43 +159,68 @@ __global__ void __launch_bounds__(kTileBlock)
   if (tile == ntiles - 1 && threadIdx.x < n)
     for (long long p = threadIdx.x; p < n; p += kTileBlock) toindex[p] = prefix + total;
   if (n <= 0) return;
-  for (long long q = threadIdx.x; q < total; q += kTileBlock) {
-    const int r = tile_find(sm, q);
-    long long rank = q - sm.loc[r];
-    const long long s = s_size[r];
-    const long long base = s_start[r];
+  // Each warp fills a contiguous share of the tile's tuples, 32 consecutive
+  // output slots per step (coalesced stores); a lane finds its list by
+  // walking forward from the list of the step's first slot.
+  constexpr int kWarps = kTileBlock / 32;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long qa = total * warp / kWarps, qb = total * (warp + 1) / kWarps;
+  if (qa >= qb) return;
+  int r = tile_find(sm, qa);
+  for (long long g = qa; g < qb; g += 32) {
+    while (sm.loc[r + 1] <= g) r++;
+    const long long q = g + lane;
+    if (q >= qb) continue;
+    int rl = r;
+    while (sm.loc[rl + 1] <= q) rl++;
+    long long rank = q - sm.loc[rl];
+    const long long s = s_size[rl];
+    const long long base = s_start[rl];
     const long long out = prefix + q;
-    if (n == 2) {
-      // first element: largest v with C(s,2) - C(s-v,2) <= rank
-      const long long tot = s * (s - 1) / 2;
-      long long lo = 0, hi = s - 2;
+    if (n == 1) {
+      s_ptr[0][out] = base + rank;
+    } else if (n == 2 && s < (1ll << 15)) {
+      int a, b;
+      unrank2_small((int)s, (int)rank, &a, &b);
+      s_ptr[0][out] = base + a;
+      s_ptr[1][out] = base + (replacement ? b - 1 : b);
+    } else if (n == 2) {
+      long long a, b;
+      unrank2(s, rank, &a, &b);
+      s_ptr[0][out] = base + a;
+      s_ptr[1][out] = base + (replacement ? b - 1 : b);
+    } else if (n == 3 && s < (1ll << 21)) {
+      // first element: largest v with C(s,3) - C(s-v,3) <= rank
+      const long long tot = binom3(s);
+      long long lo = 0, hi = s - 3;
       while (lo < hi) {
-        long long mid = (lo + hi + 1) >> 1;
-        long long m = s - mid;
-        if (tot - m * (m - 1) / 2 <= rank) lo = mid;
+        const long long mid = (lo + hi + 1) >> 1;
+        if (tot - binom3(s - mid) <= rank) lo = mid;
         else hi = mid - 1;
       }
-      const long long m = s - lo;
-      const long long a = lo;
-      const long long b2 = lo + 1 + (rank - (tot - m * (m - 1) / 2));
-      s_ptr[0][out] = base + a;
-      s_ptr[1][out] = base + (replacement ? b2 - 1 : b2);
-      continue;
-    }
-    long long lo = 0;
-    for (long long p = 0; p < n; p++) {
-      const long long rem = n - p;
-      const long long here = binom(s - lo, rem);
-      long long vlo = lo, vhi = s - rem;
-      while (vlo < vhi) {
-        long long mid = (vlo + vhi + 1) >> 1;
-        if (here - binom(s - mid, rem) <= rank) vlo = mid;
-        else vhi = mid - 1;
+      rank -= tot - binom3(s - lo);
+      long long a, b;
+      unrank2(s - lo - 1, rank, &a, &b);
+      const long long p1 = lo + 1 + a, p2 = lo + 1 + b;
+      s_ptr[0][out] = base + lo;
+      s_ptr[1][out] = base + (replacement ? p1 - 1 : p1);
+      s_ptr[2][out] = base + (replacement ? p2 - 2 : p2);
+    } else {
+      long long lo = 0;
+      for (long long p = 0; p < n; p++) {
+        const long long rem = n - p;
+        const long long here = binom(s - lo, rem);
+        long long vlo = lo, vhi = s - rem;
+        while (vlo < vhi) {
+          long long mid = (vlo + vhi + 1) >> 1;
+          if (here - binom(s - mid, rem) <= rank) vlo = mid;
+          else vhi = mid - 1;
+        }
+        rank -= here - binom(s - vlo, rem);
+        int64_t* dst = p < kMaxPtrs ? s_ptr[p] : tocarry[p];
+        dst[out] = base + (replacement ? vlo - p : vlo);
+        lo = vlo + 1;
       }
-      rank -= here - binom(s - vlo, rem);
-      int64_t* dst = p < kMaxPtrs ? s_ptr[p] : tocarry[p];
-      dst[out] = base + (replacement ? vlo - p : vlo);
-      lo = vlo + 1;
     }
   }
 }

@@ -1,0 +1,165 @@
+// jagged_chain.cu -- the two steps of jagged getitem that awkward performs with
+// cupy array operations rather than kernels of its kernel specification:
+//
+//   jagged boolean mask -> jagged local index (src/awkward/_slicing.py:476-530:
+//     localindex of the mask, boolean compaction of it, counts and their
+//     cumsum for the new offsets);
+//   content carry (NumpyArray._carry, src/awkward/contents/numpyarray.py:367-373:
+//     content[carry], a gather).
+//
+// mask_to_index: one CTA per tile of kTileLists lists.  Thread-per-list counts
+// of true entries are scanned across tiles (decoupled look-back) into the new
+// offsets; then each warp walks a contiguous share of the tile's elements 32
+// at a time, ranking the true entries with a ballot prefix, and writes the
+// local index (position within its list) of every true entry at its rank, so
+// both passes over the mask and the index writes are coalesced.
+#include "list_tile.cuh"
+
+using namespace gb;
+
+namespace {
+
+struct MaskTile {
+  long long loc[kTileLists + 1];  // list offsets relative to the tile's first element
+  long long base;
+  int count;
+};
+
+__global__ void __launch_bounds__(kTileBlock)
+    mask_to_index_kernel(int64_t* __restrict__ tooffsets, int64_t* __restrict__ toindex,
+                         const uint8_t* __restrict__ mask, const int64_t* __restrict__ offsets,
+                         long long nlists, long long ntiles, ScanTiles st, uint64_t* err) {
+  __shared__ TileSmem sm;
+  __shared__ MaskTile t;
+  const long long tile = tile_claim(sm, st);
+  const long long l0 = tile * kTileLists;
+  const long long rem = nlists - l0;
+  const int count = (int)(rem < kTileLists ? rem : kTileLists);
+  const long long base = __ldg(offsets + l0);
+  for (int i = threadIdx.x; i <= kTileLists; i += kTileBlock) {
+    const int k = i < count ? i : count;
+    t.loc[i] = __ldg(offsets + l0 + k) - base;
+  }
+  if (threadIdx.x == 0) {
+    t.base = base;
+    t.count = count;
+  }
+  __syncthreads();
+  long long c[kTileLPT];
+#pragma unroll
+  for (int r = 0; r < kTileLPT; r++) {
+    const int li = threadIdx.x * kTileLPT + r;
+    long long n = 0;
+    if (li < count)
+      for (long long j = base + t.loc[li]; j < base + t.loc[li + 1]; j++) n += mask[j] != 0;
+    c[r] = n;
+  }
+  const long long prefix = tile_scan(sm, st, tile, c, 0, err);
+  for (int li = threadIdx.x; li < kTileLists; li += kTileBlock)
+    if (li < count) tooffsets[l0 + li] = prefix + sm.loc[li];
+  if (tile == ntiles - 1 && threadIdx.x == 0) tooffsets[nlists] = prefix + sm.total;
+  // element pass
+  constexpr int kWarps = kTileBlock / 32;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long total = t.loc[count];
+  const long long qa = total * warp / kWarps, qb = total * (warp + 1) / kWarps;
+  if (qa >= qb) return;
+  int lo = 0, hi = count;  // list holding element qa: last r with loc[r] <= qa
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (t.loc[mid] <= qa) lo = mid;
+    else hi = mid;
+  }
+  int r = lo;
+  // true entries of list r before qa
+  long long before = 0;
+  for (long long q = t.loc[r] + lane; q < qa; q += 32) before += mask[base + q] != 0;
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) before += __shfl_xor_sync(0xffffffffu, before, d);
+  long long run = prefix + sm.loc[r] + before;  // rank of the next true entry
+  for (long long g = qa; g < qb; g += 32) {
+    while (t.loc[r + 1] <= g) r++;
+    const long long q = g + lane;
+    const bool in = q < qb;
+    const bool m = in && mask[base + q] != 0;
+    const unsigned b = __ballot_sync(0xffffffffu, m);
+    if (m) {
+      int rl = r;
+      while (t.loc[rl + 1] <= q) rl++;
+      toindex[run + __popc(b & ((1u << lane) - 1u))] = q - t.loc[rl];
+    }
+    run += __popc(b);
+  }
+}
+
+template <class W>
+__global__ void take_kernel(W* __restrict__ out, const W* __restrict__ content,
+                            const int64_t* __restrict__ carry, long long n, long long contentlen,
+                            uint64_t inv, uint64_t* err) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long c = __ldg(carry + i);
+    if (c < 0 || c >= contentlen) {
+      raise_error(err, inv, 0);
+      continue;
+    }
+    out[i] = __ldg(content + c);
+  }
+}
+
+}  // namespace
+
+// The new offsets (nlists + 1 entries) and, for each true entry of the mask
+// in order, its position within its list.  toindex must hold as many entries
+// as the mask has true values in the offsets' span (at most offsets[nlists] -
+// offsets[0]).
+GB_EXPORT int awkward_gb300_jagged_mask_to_index(int64_t* tooffsets, int64_t* toindex,
+                                                 const uint8_t* mask, const int64_t* offsets,
+                                                 int64_t nlists, uint64_t* err_code,
+                                                 void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (nlists <= 0) return (int)cudaMemsetAsync(tooffsets, 0, sizeof(int64_t), s);
+  const long long nt = tile_count(nlists);
+  ScanTiles st;
+  void* scratch = nullptr;
+  cudaError_t e = scan_tiles_alloc(&st, &scratch, nt, s);
+  if (e != cudaSuccess) return (int)e;
+  mask_to_index_kernel<<<(unsigned)nt, kTileBlock, 0, s>>>(tooffsets, toindex, mask, offsets,
+                                                           nlists, nt, st, err_code);
+  e = cudaGetLastError();
+  cudaError_t f = scratch_free(scratch, s);
+  return (int)(e != cudaSuccess ? e : f);
+}
+
+// out[i] = content[carry[i]] for element widths of 1, 2, 4 and 8 bytes; a carry
+// outside [0, contentlen) raises code 0 ("index out of range").
+GB_EXPORT int awkward_gb300_take(void* out, const void* content, int64_t itemsize,
+                                 const int64_t* carry, int64_t n, int64_t contentlen,
+                                 uint64_t invocation_index, uint64_t* err_code, void* stream) {
+  if (n <= 0) return 0;
+  long long g = (n + 255) / 256;
+  const long long cap = (long long)device_sm_count() * 32;
+  const unsigned grid = (unsigned)(g < cap ? g : cap);
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (itemsize) {
+    case 1:
+      take_kernel<uint8_t><<<grid, 256, 0, s>>>((uint8_t*)out, (const uint8_t*)content, carry, n,
+                                                contentlen, invocation_index, err_code);
+      break;
+    case 2:
+      take_kernel<uint16_t><<<grid, 256, 0, s>>>((uint16_t*)out, (const uint16_t*)content, carry,
+                                                 n, contentlen, invocation_index, err_code);
+      break;
+    case 4:
+      take_kernel<uint32_t><<<grid, 256, 0, s>>>((uint32_t*)out, (const uint32_t*)content, carry,
+                                                 n, contentlen, invocation_index, err_code);
+      break;
+    case 8:
+      take_kernel<uint64_t><<<grid, 256, 0, s>>>((uint64_t*)out, (const uint64_t*)content, carry,
+                                                 n, contentlen, invocation_index, err_code);
+      break;
+    default:
+      return (int)cudaErrorInvalidValue;
+  }
+  return (int)cudaGetLastError();
+}

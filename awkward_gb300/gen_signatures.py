@@ -232,28 +232,10 @@ def main(refroot):
         h.append(
             f"int {name}({decl}, uint64_t invocation_index, uint64_t* err_code, void* stream);"
         )
+    from ._extensions import header_lines
+
+    h += header_lines()
     h += [
-        "",
-        "/* ---- no-alloc variant.  No counterpart in awkward: an extra entry point",
-        " * of this library for callers that may not allocate device memory while",
-        " * they run, e.g. code embedded in a process whose GPU memory is owned by",
-        " * another framework's pooling allocator (cudaMalloc then fails or goes",
-        " * around the pool, and the caller has no handle to the pool).",
-        " * Same arguments and results as awkward_ListArray64_getitem_jagged_apply_64;",
-        " * its tile-state scratch is a fixed 512 KiB device array inside the",
-        " * library (held on every GPU that loads it until exit) instead of a",
-        " * pool allocation.  sliceouterlen above AWKWARD_GB300_NOALLOC_MAX_LISTS",
-        " * returns cudaErrorInvalidValue (1) and launches nothing.  All calls",
-        " * share the array: calls that overlap on the GPU (other streams or",
-        " * threads) race and must be ordered by the caller.  The first call on",
-        " * each device looks up the array's device address, so make it before",
-        " * any stream capture on that device. */",
-        "#define AWKWARD_GB300_NOALLOC_MAX_LISTS 67108864LL",
-        "int awkward_ListArray64_getitem_jagged_apply_64_noalloc(int64_t* tooffsets, int64_t* tocarry, "
-        "const int64_t* slicestarts, const int64_t* slicestops, int64_t sliceouterlen, "
-        "const int64_t* sliceindex, int64_t sliceinnerlen, const int64_t* fromstarts, "
-        "const int64_t* fromstops, int64_t contentlen, uint64_t invocation_index, "
-        "uint64_t* err_code, void* stream);",
         "",
         "#ifdef __cplusplus",
         "}",

@@ -241,6 +241,66 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _time_ms(fn, reps, stream):
+    """Mean device time of fn() over reps launches (CUDA events on `stream`)."""
+    import torch
+
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record(stream)
+    for _ in range(reps):
+        fn()
+    b.record(stream)
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def measure_c3(be, dev, reps, warmup, n_lists=5_000_000, n3_lists=1_000_000):
+    """ak.combinations(axis=1): n=2 on lists of min(Poisson(6), 40), n=3 on Poisson(4).
+
+    Per configuration: combinations_length (tuple counts, offsets, total)
+    then combinations (the n carries), inputs resident; tuples/s over both
+    kernels; algorithmic bytes of the fill 16N + 8(N+1) + 8nP.
+    """
+    import torch
+
+    res = {}
+    stream = torch.cuda.current_stream(dev)
+    for n, nl, lam, cap, seed in ((2, n_lists, 6, 40, 3), (3, n3_lists, 4, None, 4)):
+        rng = np.random.default_rng(seed)
+        L = rng.poisson(lam, nl)
+        if cap:
+            L = np.minimum(L, cap)
+        off = torch.from_numpy(np.concatenate([[0], np.cumsum(L)]).astype(np.int64)).to(dev)
+        st, sp = off[:-1].contiguous(), off[1:].contiguous()
+        tot = torch.empty(1, dtype=torch.int64, device=dev)
+        too = torch.empty(nl + 1, dtype=torch.int64, device=dev)
+        kl = be["awkward_ListArray_combinations_length", np.int64, np.int64, np.int64, np.int64]
+        kc = be["awkward_ListArray_combinations", np.int64, np.int64, np.int64, np.int64, np.int64]
+        kl(tot, too, n, False, st, sp, nl)
+        be.synchronize()
+        P = int(tot.item())
+        rows = [torch.empty(P, dtype=torch.int64, device=dev) for _ in range(n)]
+        ti = torch.empty(n, dtype=torch.int64, device=dev)
+        fi = torch.zeros(n, dtype=torch.int64, device=dev)
+        for _ in range(max(warmup, 3)):
+            kl(tot, too, n, False, st, sp, nl)
+            kc(rows, ti, fi, n, False, st, sp, nl)
+        be.synchronize()
+        t_len = _time_ms(lambda: kl(tot, too, n, False, st, sp, nl), reps, stream)
+        t_fill = _time_ms(lambda: kc(rows, ti, fi, n, False, st, sp, nl), reps, stream)
+        be.synchronize()
+        fill_bytes = 16 * nl + 8 * (nl + 1) + 8 * n * P
+        res[f"n{n}"] = {
+            "lists": nl, "tuples": P,
+            "tuples_per_s": round(P / ((t_len + t_fill) * 1e-3), 1),
+            "length_us": round(t_len * 1e3, 1), "fill_us": round(t_fill * 1e3, 1),
+            "fill_gbs": round(fill_bytes / (t_fill * 1e-3) / 1e9, 1),
+            "lengths": f"min(Poisson({lam}), {cap})" if cap else f"Poisson({lam})",
+        }
+        del rows
+    return res
+
+
 def run_gb300(args):
     import torch
 
@@ -249,6 +309,13 @@ def run_gb300(args):
     rank, world, local = dist_setup(args.gpus)
     dev = torch.device("cuda", torch.cuda.current_device())
     be = awkward_gb300.backend()
+    if args.only == "c3":
+        n2 = args.lists or 5_000_000
+        print(json.dumps({"c3_combinations": measure_c3(be, dev, args.steps, args.warmup, n2,
+                                                        max(n2 // 5, 1))}))
+        return
+    if args.lists is None:
+        args.lists = N_LISTS
     k_sum = be["awkward_reduce_sum", np.float64, np.float64, np.int64]
     k_max = be["awkward_reduce_max", np.float64, np.float64, np.int64]
     k_arg = be["awkward_reduce_argmax", np.int64, np.float64, np.int64, np.int64]
@@ -370,6 +437,8 @@ def run_gb300(args):
         "gpu_launches": args.steps * 3 * 2,
         "clocks": sampler.summary(),
     }
+    if rank == 0 and not args.no_extras:
+        line["c3_combinations"] = measure_c3(be, dev, max(args.steps // 2, 5), args.warmup)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(2_000_000, 1, 8.0).items()
                                 if k != "ms_per_step"}
@@ -388,11 +457,17 @@ def main():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--lists", type=int, default=N_LISTS,
-                   help="list count (default: the 10M-list headline workload; smaller "
-                        "values are for profiling captures)")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the secondary workloads (combinations, ...)")
+    p.add_argument("--only", default=None, choices=["c3"],
+                   help="run one secondary workload alone (profiling); --lists sets its size")
+    p.add_argument("--lists", type=int, default=None,
+                   help="list count (default: 10M lists for the reducers, 5M for --only c3; "
+                        "smaller values are for profiling captures)")
     args = p.parse_args()
     if args.impl == "reference":
+        if args.lists is None:
+            args.lists = N_LISTS
         run_reference(args)
     else:
         run_gb300(args)

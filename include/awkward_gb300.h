@@ -448,6 +448,38 @@ int awkward_reduce_sum_int64_bool_64(int64_t* toptr, const bool* fromptr, const 
 #define AWKWARD_GB300_NOALLOC_MAX_LISTS 67108864LL
 int awkward_ListArray64_getitem_jagged_apply_64_noalloc(int64_t* tooffsets, int64_t* tocarry, const int64_t* slicestarts, const int64_t* slicestops, int64_t sliceouterlen, const int64_t* sliceindex, int64_t sliceinnerlen, const int64_t* fromstarts, const int64_t* fromstops, int64_t contentlen, uint64_t invocation_index, uint64_t* err_code, void* stream);
 
+/* ---- jagged getitem steps that awkward performs with cupy array operations
+ * instead of kernels of its specification (no counterpart in
+ * kernel-specification.yml):
+ *   jagged_mask_to_index: jagged boolean mask (uint8, one byte per element,
+ *     indexed globally over offsets[0]..offsets[nlists]) -> new offsets
+ *     [nlists + 1] and, for each true entry in order, its position within its
+ *     list (src/awkward/_slicing.py:476-530: localindex + compaction + cumsum);
+ *   take: out[i] = content[carry[i]] for itemsize 1, 2, 4 or 8 bytes
+ *     (NumpyArray._carry); a carry outside [0, contentlen) sets err_code to
+ *     invocation_index*256 + 0 ("index out of range"). */
+int awkward_gb300_jagged_mask_to_index(int64_t* tooffsets, int64_t* toindex, const uint8_t* mask, const int64_t* offsets, int64_t nlists, uint64_t* err_code, void* stream);
+int awkward_gb300_take(void* out, const void* content, int64_t itemsize, const int64_t* carry, int64_t n, int64_t contentlen, uint64_t invocation_index, uint64_t* err_code, void* stream);
+
+/* ---- backward kernels of differentiable jagged operations (torch.autograd
+ * in awkward_gb300/autograd.py).  No counterpart in awkward, which has no
+ * CUDA backward kernels.  Pointers are device pointers; offsets are int64
+ * [nlists + 1] (need not start at 0); element arrays are indexed globally.
+ *   segment_sum_backward:   grad_x[j] = grad_out[list of j]
+ *   segment_max_backward:   grad_x = 0; grad_x[argmax[l]] = grad_out[l] for
+ *                           argmax[l] in [0, nelements) (global indices, -1 empty)
+ *   jagged_softmax_forward: y = exp(x - max) / sum(exp(x - max)) per list
+ *   jagged_softmax_backward: grad_x = y * (grad_y - sum(grad_y * y)) per list,
+ *                           y from y_saved, or recomputed from x when NULL */
+int awkward_gb300_segment_sum_backward_float32(float* grad_x, const float* grad_out, const int64_t* offsets, int64_t nlists, void* stream);
+int awkward_gb300_segment_max_backward_float32(float* grad_x, const float* grad_out, const int64_t* argmax, int64_t nelements, int64_t nlists, void* stream);
+int awkward_gb300_jagged_softmax_forward_float32(float* y, const float* x, const int64_t* offsets, int64_t nlists, void* stream);
+int awkward_gb300_jagged_softmax_backward_float32(float* grad_x, const float* grad_y, const float* x, const float* y_saved, const int64_t* offsets, int64_t nlists, void* stream);
+int awkward_gb300_segment_sum_backward_float64(double* grad_x, const double* grad_out, const int64_t* offsets, int64_t nlists, void* stream);
+int awkward_gb300_segment_max_backward_float64(double* grad_x, const double* grad_out, const int64_t* argmax, int64_t nelements, int64_t nlists, void* stream);
+int awkward_gb300_jagged_softmax_forward_float64(double* y, const double* x, const int64_t* offsets, int64_t nlists, void* stream);
+int awkward_gb300_jagged_softmax_backward_float64(double* grad_x, const double* grad_y, const double* x, const double* y_saved, const int64_t* offsets, int64_t nlists, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,214 @@
+"""GPU parity of the jagged slicing chain (array[mask], array[idx], array[..., 1:]).
+
+* ``jagged_mask_to_index`` against numpy (positions of true entries within
+  their lists, offsets = cumulative counts), bit-exact, including empty lists,
+  offsets not starting at 0, an all-true / all-false mask and a 100,000-element
+  list;
+* ``take`` against numpy for 1, 2, 4 and 8-byte items, and its range error;
+* the whole chains at moderate size against the C oracle's
+  ``jagged_apply`` / ``next_range`` and numpy gathers, bit-exact;
+* at the full jagged-slicing size (10,000,000 lists, Poisson(8), float32
+  content), exact properties: the mask chain's carry equals the positions of
+  the true entries, the index chain's carry equals start + (idx mod len), and
+  the [..., 1:] chain keeps every inner element but the first.
+"""
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _case(nl, seed, lam=8, base=0, extra=None, p=0.4):
+    rng = np.random.default_rng(seed)
+    L = rng.poisson(lam, nl)
+    L[rng.random(nl) < 0.01] = 0
+    if extra is not None:
+        L = np.concatenate([L, extra])
+    off = (np.concatenate([[0], np.cumsum(L)]) + base).astype(np.int64)
+    x = (rng.exponential(1.0, int(off[-1])) * 20).astype(np.float32)
+    mask = rng.random(int(off[-1])) < p
+    return rng, L, off, x, mask
+
+
+def _np_mask_index(off, mask):
+    L = np.diff(off)
+    counts = np.add.reduceat(mask[off[0]:].astype(np.int64), off[:-1] - off[0]) * (L > 0) if len(L) else np.zeros(0, np.int64)
+    ioff = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    owner = np.repeat(np.arange(len(L)), L)
+    local = np.arange(int(off[-1] - off[0])) - (off[:-1] - off[0])[owner]
+    return ioff, local[mask[off[0]:]].astype(np.int64)
+
+
+@pytest.mark.parametrize("variant", ["poisson", "base", "all_true", "all_false", "long_list"])
+def test_mask_to_index_matches_numpy(variant):
+    import torch
+
+    from awkward_gb300 import jagged
+
+    kw = {"poisson": {}, "base": {"base": 7}, "all_true": {"p": 1.1}, "all_false": {"p": -1},
+          "long_list": {"extra": np.array([0, 100_000, 3])}}[variant]
+    _rng, _L, off, _x, mask = _case(50_000, 11, **kw)
+    ioff, idx = jagged.jagged_mask_to_index(torch.from_numpy(off).cuda(),
+                                            torch.from_numpy(mask).cuda())
+    e_ioff, e_idx = _np_mask_index(off, mask)
+    np.testing.assert_array_equal(ioff.cpu().numpy(), e_ioff)
+    np.testing.assert_array_equal(idx.cpu().numpy(), e_idx)
+
+
+@pytest.mark.parametrize("dt", [np.int8, np.int16, np.float32, np.float64])
+def test_take_matches_numpy(dt):
+    import torch
+
+    from awkward_gb300 import jagged
+
+    rng = np.random.default_rng(5)
+    content = rng.integers(-100, 100, 100_003).astype(dt)
+    carry = rng.integers(0, len(content), 777_777).astype(np.int64)
+    got = jagged.take(torch.from_numpy(content).cuda(), torch.from_numpy(carry).cuda())
+    np.testing.assert_array_equal(got.cpu().numpy(), content[carry])
+    with pytest.raises(ValueError, match="index out of range"):
+        jagged.take(torch.from_numpy(content).cuda(),
+                    torch.tensor([0, len(content)], dtype=torch.int64, device="cuda"))
+
+
+def _oracle_apply(off, ioff, idx):
+    n = len(off) - 1
+    too = np.zeros(n + 1, np.int64)
+    toc = np.zeros(max(len(idx), 1), np.int64)
+    msg = oracle.call(oracle.load(), "awkward_ListArray64_getitem_jagged_apply_64", tooffsets=too,
+                      tocarry=toc, slicestarts=ioff[:-1].copy(), slicestops=ioff[1:].copy(),
+                      sliceouterlen=n, sliceindex=idx, sliceinnerlen=len(idx),
+                      fromstarts=off[:-1].copy(), fromstops=off[1:].copy(),
+                      contentlen=int(off[-1]))[0]
+    assert msg is None
+    return too, toc[: len(idx)]
+
+
+def test_mask_chain_matches_oracle():
+    import torch
+
+    from awkward_gb300 import jagged
+
+    _rng, _L, off, x, mask = _case(200_000, 12, base=3)
+    too, content = jagged.getitem_jagged_mask(torch.from_numpy(off).cuda(),
+                                              torch.from_numpy(x).cuda(),
+                                              torch.from_numpy(mask).cuda())
+    ioff, idx = _np_mask_index(off, mask)
+    e_too, e_carry = _oracle_apply(off, ioff, idx)
+    np.testing.assert_array_equal(too.cpu().numpy(), e_too)
+    np.testing.assert_array_equal(content.cpu().numpy(), x[e_carry])
+
+
+def _index_case(rng, L):
+    K = np.where(L > 0, rng.poisson(2, len(L)), 0)
+    ioff = np.concatenate([[0], np.cumsum(K)]).astype(np.int64)
+    idx = np.concatenate([rng.integers(-l, l, k) for l, k in zip(L, K) if k] or
+                         [np.zeros(0, np.int64)]).astype(np.int64)
+    return ioff, idx
+
+
+def test_index_chain_matches_oracle():
+    import torch
+
+    from awkward_gb300 import jagged
+
+    rng, L, off, x, _mask = _case(200_000, 13)
+    ioff, idx = _index_case(rng, L)
+    too, content = jagged.getitem_jagged_index(torch.from_numpy(off).cuda(),
+                                               torch.from_numpy(x).cuda(),
+                                               torch.from_numpy(ioff).cuda(),
+                                               torch.from_numpy(idx).cuda())
+    e_too, e_carry = _oracle_apply(off, ioff, idx)
+    np.testing.assert_array_equal(too.cpu().numpy(), e_too)
+    np.testing.assert_array_equal(content.cpu().numpy(), x[e_carry])
+
+
+def test_index_chain_error_is_awkwards():
+    import torch
+
+    from awkward_gb300 import jagged
+
+    off = torch.tensor([0, 2, 5], dtype=torch.int64, device="cuda")
+    x = torch.zeros(5, dtype=torch.float32, device="cuda")
+    ioff = torch.tensor([0, 1, 2], dtype=torch.int64, device="cuda")
+    idx = torch.tensor([0, 3], dtype=torch.int64, device="cuda")  # 3 >= len 3
+    with pytest.raises(ValueError, match="index out of range"):
+        jagged.getitem_jagged_index(off, x, ioff, idx)
+
+
+@pytest.mark.parametrize("start,stop,step", [(1, None, None), (None, -1, None), (1, None, 2),
+                                             (None, None, -1), (-2, 0, -1)])
+def test_inner_range_matches_oracle(start, stop, step):
+    import torch
+
+    from awkward_gb300 import jagged
+
+    rng = np.random.default_rng(14)
+    Lo = rng.poisson(4, 100_000)
+    Li = rng.poisson(6, int(Lo.sum()))
+    inner = np.concatenate([[0], np.cumsum(Li)]).astype(np.int64)
+    x = rng.standard_normal(int(inner[-1])).astype(np.float32)
+    nxo, nxc = jagged.inner_range(torch.from_numpy(inner).cuda(), start, stop, step)
+    n = len(inner) - 1
+    none = jagged.SLICE_NONE
+    a = none if start is None else start
+    b = none if stop is None else stop
+    c = 1 if step is None else step
+    lib = oracle.load()
+    cl = np.zeros(1, np.int64)
+    assert oracle.call(lib, "awkward_ListArray64_getitem_next_range_carrylength", carrylength=cl,
+                       fromstarts=inner[:-1].copy(), fromstops=inner[1:].copy(), lenstarts=n,
+                       start=a, stop=b, step=c)[0] is None
+    e_off = np.zeros(n + 1, np.int64)
+    e_carry = np.zeros(max(int(cl[0]), 1), np.int64)
+    assert oracle.call(lib, "awkward_ListArray64_getitem_next_range_64", tooffsets=e_off,
+                       tocarry=e_carry, fromstarts=inner[:-1].copy(), fromstops=inner[1:].copy(),
+                       lenstarts=n, start=a, stop=b, step=c)[0] is None
+    np.testing.assert_array_equal(nxo.cpu().numpy(), e_off)
+    np.testing.assert_array_equal(nxc.cpu().numpy(), e_carry[: int(cl[0])])
+    got = jagged.take(torch.from_numpy(x).cuda(), nxc)
+    np.testing.assert_array_equal(got.cpu().numpy(), x[e_carry[: int(cl[0])]])
+
+
+def test_full_size_chains_properties():
+    import torch
+
+    from awkward_gb300 import jagged
+
+    rng, L, off, x, mask = _case(10_000_000, 15)
+    d_off = torch.from_numpy(off).cuda()
+    d_x = torch.from_numpy(x).cuda()
+    d_mask = torch.from_numpy(mask).cuda()
+    owner = torch.repeat_interleave(torch.arange(len(L), device="cuda"),
+                                    torch.from_numpy(L).cuda())
+    # array[mask]: carry = positions of the true entries, offsets = cumulative counts
+    ioff, idx = jagged.jagged_mask_to_index(d_off, d_mask)
+    too, tocarry = jagged.jagged_apply(d_off, ioff, idx, d_x.numel())
+    assert torch.equal(tocarry, torch.nonzero(d_mask).flatten())
+    counts = torch.zeros(len(L), dtype=torch.int64, device="cuda").index_add_(
+        0, owner, d_mask.to(torch.int64))
+    assert torch.equal(too[1:] - too[:-1], counts)
+    assert torch.equal(jagged.take(d_x, tocarry), d_x[d_mask])
+    # array[idx]: carry = start + (idx mod len)
+    ioff_h, idx_h = _index_case(rng, L)
+    d_ioff, d_idx = torch.from_numpy(ioff_h).cuda(), torch.from_numpy(idx_h).cuda()
+    too2, tocarry2 = jagged.jagged_apply(d_off, d_ioff, d_idx, d_x.numel())
+    iowner = torch.repeat_interleave(torch.arange(len(L), device="cuda"),
+                                     d_ioff[1:] - d_ioff[:-1])
+    Ld = (d_off[1:] - d_off[:-1])[iowner]
+    assert torch.equal(tocarry2, d_off[:-1][iowner] + torch.remainder(d_idx, Ld))
+    assert torch.equal(too2, d_ioff)
+    # two-level [..., 1:]: every inner element but the first
+    Lo = rng.poisson(4, 10_000_000)
+    Li = rng.poisson(6, int(Lo.sum()))
+    inner = torch.from_numpy(np.concatenate([[0], np.cumsum(Li)]).astype(np.int64)).cuda()
+    nxo, nxc = jagged.inner_range(inner, 1, None, None)
+    keep = torch.ones(int(inner[-1]), dtype=torch.bool, device="cuda")
+    starts = inner[:-1][(inner[1:] - inner[:-1]) > 0]
+    keep[starts] = False
+    assert torch.equal(nxc, torch.nonzero(keep).flatten())
+    Lt = torch.from_numpy(Li).cuda()
+    assert torch.equal(nxo[1:] - nxo[:-1], torch.clamp(Lt - 1, min=0))

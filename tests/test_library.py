@@ -10,8 +10,10 @@ from awkward_gb300._signatures import SIGNATURES
 from awkward_gb300.kernel_table import GB300Backend, kernel_key
 
 
-# The one entry point without a kernel-specification.yml counterpart.
-EXTRA = {"awkward_ListArray64_getitem_jagged_apply_64_noalloc"}
+from awkward_gb300._extensions import EXTENSIONS
+
+# Entry points without a kernel-specification.yml counterpart.
+EXTRA = set(EXTENSIONS)
 
 
 def _header_names():
@@ -34,6 +36,8 @@ def test_library_builds_loads_and_exports_every_declaration():
     assert "sm_103a" in _abi.version()
     for n in SIGNATURES:  # argtypes resolve for every entry point
         _abi.cfunc(n)
+    for n in EXTENSIONS:
+        _abi.ext_cfunc(n)
 
 
 def test_kernel_keys_follow_awkward_scheme():
