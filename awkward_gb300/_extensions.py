@@ -79,15 +79,37 @@ EXTENSIONS["awkward_gb300_take"] = (
      ("const int64_t*", "carry"), ("int64_t", "n"), ("int64_t", "contentlen"),
      ("uint64_t", "invocation_index"), ("uint64_t*", "err_code"), ("void*", "stream")], "jagged")
 
+_BATCH_COMMENT = """batched execution (no counterpart in awkward): sum, max, argmax and
+count (axis=-1) and array[mask] of many float64 ListOffsetArrays in one
+launch per operation.  plan_create (set-up: allocates and uploads the
+work-queue tables, synchronous) takes host arrays of narrays entries:
+list counts, element counts (offsets[n] - offsets[0]) and the device
+pointers of each array's content, offsets, uint8 mask and outputs
+(out_sum/out_max [n] float64, out_argmax/out_count [n] int64,
+sel_offsets [n + 1] int64, sel_content [elements] float64).  Reducer
+results are bit-identical to the per-array entry points.  plan_run only
+launches (capturable in a CUDA graph); plan_destroy frees the plan."""
+
+EXTENSIONS["awkward_gb300_batch_plan_create"] = (
+    [("void**", "plan"), ("int64_t", "narrays"), ("const int64_t*", "nlists"),
+     ("const int64_t*", "nelements"), ("const double* const*", "x"),
+     ("const int64_t* const*", "offsets"), ("const uint8_t* const*", "mask"),
+     ("double* const*", "out_sum"), ("double* const*", "out_max"),
+     ("int64_t* const*", "out_argmax"), ("int64_t* const*", "out_count"),
+     ("int64_t* const*", "sel_offsets"), ("double* const*", "sel_content"),
+     ("int64_t", "order_mode"), ("int64_t", "occupancy_div"), ("uint64_t*", "err_code")], "batch")
+EXTENSIONS["awkward_gb300_batch_plan_run"] = ([("void*", "plan"), ("void*", "stream")], "batch")
+EXTENSIONS["awkward_gb300_batch_plan_destroy"] = ([("void*", "plan")], "batch")
+
 GROUP_COMMENTS = {"noalloc": _NOALLOC_COMMENT, "autograd": _AUTOGRAD_COMMENT,
-                  "jagged": _JAGGED_COMMENT}
+                  "jagged": _JAGGED_COMMENT, "batch": _BATCH_COMMENT}
 GROUP_DEFINES = {"noalloc": ["#define AWKWARD_GB300_NOALLOC_MAX_LISTS 67108864LL"]}
 
 
 def header_lines():
     """Declarations of the extension entry points, grouped, for the C header."""
     out = []
-    for group in ("noalloc", "jagged", "autograd"):
+    for group in ("noalloc", "jagged", "autograd", "batch"):
         out.append("")
         text = GROUP_COMMENTS[group].splitlines()
         out.append(f"/* ---- {text[0]}")

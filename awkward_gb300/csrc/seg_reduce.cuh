@@ -134,24 +134,17 @@ __device__ __forceinline__ T ld_ro(const T* p) {
   return __ldg(p);
 }
 
-template <class Op>
-__global__ void __launch_bounds__(kSegBlock, kSegMinBlocks)
-    seg_reduce_kernel(Op op, const store_t<typename Op::In>* __restrict__ x,
-                      const int64_t* __restrict__ offsets, long long nlists,
-                      typename Op::Out* __restrict__ out, RangeRecord<typename Op::Acc>* records,
-                      int W, uint64_t inv, uint64_t* err) {
-  (void)inv;
-  (void)err;
+// Reduce the lists of merge-path diagonal range [d0, d1) of one array
+// (whole warp).  emit(list, acc) delivers each list reduced entirely here;
+// the partials of lists crossing the range ends go to `rec`.
+template <class Op, class Emit>
+__device__ __forceinline__ void seg_reduce_range(const Op& op,
+                                                 const store_t<typename Op::In>* __restrict__ x,
+                                                 const int64_t* __restrict__ offsets,
+                                                 long long nlists, long long e0, long long E,
+                                                 long long d0, long long d1, Emit emit,
+                                                 RangeRecord<typename Op::Acc>& rec) {
   const int lane = threadIdx.x & 31;
-  const int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
-  const long long e0 = __ldg(offsets);
-  const long long eN = __ldg(offsets + nlists);
-  const long long E = eN > e0 ? eN - e0 : 0;
-  const long long D = nlists + E;
-  const long long wanted = (D + kMinRangeItems - 1) / kMinRangeItems;
-  const int Weff = (int)(wanted < W ? wanted : W);
-  if (w >= Weff) return;
-  const long long d0 = D * w / Weff, d1 = D * (w + 1) / Weff;
   // both ends at once: lanes 0-15 search d0, lanes 16-31 search d1
   const bool upper = lane >= 16;
   const long long split = mp_search_half(offsets, nlists, e0, E, upper ? d1 : d0,
@@ -192,23 +185,53 @@ __global__ void __launch_bounds__(kSegBlock, kSegMinBlocks)
     }
     if (act && !skip) {
       if (li == I1) {
-        records[w].tail_acc = acc;  // a giant list continues in the next range
+        rec.tail_acc = acc;  // a giant list continues in the next range
       } else if (s0 > st) {
-        records[w].head_acc = acc;  // the end of a giant list that began earlier
+        rec.head_acc = acc;  // the end of a giant list that began earlier
       } else {
-        out[li] = op.finalize(acc, li);
+        emit(li, acc);
       }
     }
   }
   if (lane == 0) {
     const long long st0 = __ldg(offsets + I0);
     const bool head = I0 < I1 && st0 < J0 && __ldg(offsets + I0 + 1) - st0 > kAbsorb;
-    records[w].head_list = head ? I0 : -1;
+    rec.head_list = head ? I0 : -1;
     const bool tail = I1 < nlists && __ldg(offsets + I1 + 1) - __ldg(offsets + I1) > kAbsorb;
-    records[w].tail_list = tail ? I1 : -1;
-    records[w].tail_fresh = (tail && __ldg(offsets + I1) >= J0) ? 1 : 0;
-    if (!tail) records[w].tail_acc = op.identity();
+    rec.tail_list = tail ? I1 : -1;
+    rec.tail_fresh = (tail && __ldg(offsets + I1) >= J0) ? 1 : 0;
+    if (!tail) rec.tail_acc = op.identity();
   }
+}
+
+// Number of warp ranges an array of nlists lists and E elements is split
+// into when W warps are available (the batched path uses the same split, so
+// both give bit-identical results).
+__host__ __device__ __forceinline__ int seg_ranges(long long nlists, long long E, int W) {
+  const long long D = nlists + E;
+  const long long wanted = (D + kMinRangeItems - 1) / kMinRangeItems;
+  return (int)(wanted < W ? wanted : W);
+}
+
+template <class Op>
+__global__ void __launch_bounds__(kSegBlock, kSegMinBlocks)
+    seg_reduce_kernel(Op op, const store_t<typename Op::In>* __restrict__ x,
+                      const int64_t* __restrict__ offsets, long long nlists,
+                      typename Op::Out* __restrict__ out, RangeRecord<typename Op::Acc>* records,
+                      int W, uint64_t inv, uint64_t* err) {
+  (void)inv;
+  (void)err;
+  const int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+  const long long e0 = __ldg(offsets);
+  const long long eN = __ldg(offsets + nlists);
+  const long long E = eN > e0 ? eN - e0 : 0;
+  const long long D = nlists + E;
+  const int Weff = seg_ranges(nlists, E, W);
+  if (w >= Weff) return;
+  const long long d0 = D * w / Weff, d1 = D * (w + 1) / Weff;
+  seg_reduce_range(
+      op, x, offsets, nlists, e0, E, d0, d1,
+      [&](long long li, const typename Op::Acc& a) { out[li] = op.finalize(a, li); }, records[w]);
 }
 
 // Giant lists (more than kAbsorb elements) that cross warp ranges: one warp
@@ -224,9 +247,7 @@ __global__ void __launch_bounds__(256)
   const int lane = threadIdx.x & 31;
   const long long e0 = __ldg(offsets), eN = __ldg(offsets + nlists);
   const long long E = eN > e0 ? eN - e0 : 0;
-  const long long D = nlists + E;
-  const long long wanted = (D + kMinRangeItems - 1) / kMinRangeItems;
-  const int Weff = (int)(wanted < W ? wanted : W);
+  const int Weff = seg_ranges(nlists, E, W);
   const int c0 = (int)(((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5) * 32);
   if (c0 >= Weff) return;
   const int c = c0 + lane;

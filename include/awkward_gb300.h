@@ -480,6 +480,20 @@ int awkward_gb300_segment_max_backward_float64(double* grad_x, const double* gra
 int awkward_gb300_jagged_softmax_forward_float64(double* y, const double* x, const int64_t* offsets, int64_t nlists, void* stream);
 int awkward_gb300_jagged_softmax_backward_float64(double* grad_x, const double* grad_y, const double* x, const double* y_saved, const int64_t* offsets, int64_t nlists, void* stream);
 
+/* ---- batched execution (no counterpart in awkward): sum, max, argmax and
+ * count (axis=-1) and array[mask] of many float64 ListOffsetArrays in one
+ * launch per operation.  plan_create (set-up: allocates and uploads the
+ * work-queue tables, synchronous) takes host arrays of narrays entries:
+ * list counts, element counts (offsets[n] - offsets[0]) and the device
+ * pointers of each array's content, offsets, uint8 mask and outputs
+ * (out_sum/out_max [n] float64, out_argmax/out_count [n] int64,
+ * sel_offsets [n + 1] int64, sel_content [elements] float64).  Reducer
+ * results are bit-identical to the per-array entry points.  plan_run only
+ * launches (capturable in a CUDA graph); plan_destroy frees the plan. */
+int awkward_gb300_batch_plan_create(void** plan, int64_t narrays, const int64_t* nlists, const int64_t* nelements, const double* const* x, const int64_t* const* offsets, const uint8_t* const* mask, double* const* out_sum, double* const* out_max, int64_t* const* out_argmax, int64_t* const* out_count, int64_t* const* sel_offsets, double* const* sel_content, int64_t order_mode, int64_t occupancy_div, uint64_t* err_code);
+int awkward_gb300_batch_plan_run(void* plan, void* stream);
+int awkward_gb300_batch_plan_destroy(void* plan);
+
 #ifdef __cplusplus
 }
 #endif
