@@ -301,6 +301,184 @@ def measure_c3(be, dev, reps, warmup, n_lists=5_000_000, n3_lists=1_000_000):
     return res
 
 
+def measure_c2(be, dev, reps, warmup, n_lists=10_000_000):
+    """Jagged slicing at 10M lists (Poisson(8), float32 content ~ Exp(1)*20, seed 1):
+    array[mask] (Bernoulli(0.4) jagged mask), array[idx] (per list Poisson(2)
+    int64 indices in [-len, len)), and [..., 1:] on a two-level array (10M outer
+    lists of Poisson(4) inner lists of Poisson(6)).  Device time of each chain's
+    kernels with outputs pre-sized (the sizes awkward reads back are read once
+    before timing)."""
+    import torch
+
+    from awkward_gb300 import _abi, jagged
+
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+    gen = torch.Generator(device=dev).manual_seed(1)
+    L = torch.poisson(torch.full((n_lists,), 8.0, device=dev), generator=gen).to(torch.int64)
+    off = torch.zeros(n_lists + 1, dtype=torch.int64, device=dev)
+    torch.cumsum(L, 0, out=off[1:])
+    E = int(off[-1].item())
+    x = (torch.empty(E, device=dev).exponential_(1.0, generator=gen) * 20).to(torch.float32)
+    mask = torch.rand(E, device=dev, generator=gen) < 0.4
+    K = torch.where(L > 0, torch.poisson(torch.full((n_lists,), 2.0, device=dev), generator=gen),
+                    torch.zeros((), device=dev)).to(torch.int64)
+    ioff = torch.zeros(n_lists + 1, dtype=torch.int64, device=dev)
+    torch.cumsum(K, 0, out=ioff[1:])
+    owner = torch.repeat_interleave(torch.arange(n_lists, device=dev), K)
+    Lk = L[owner]
+    idx = (torch.rand(owner.numel(), device=dev, generator=gen) * (2 * Lk)).to(torch.int64) - Lk
+    err = torch.full((1,), -1, dtype=torch.int64, device=dev)
+    f_m2i = _abi.ext_cfunc("awkward_gb300_jagged_mask_to_index")
+    f_take = _abi.ext_cfunc("awkward_gb300_take")
+    k_apply = be["awkward_ListArray_getitem_jagged_apply", np.int64, np.int64, np.int64, np.int64,
+                 np.int64, np.int64, np.int64]
+    starts, stops = off[:-1].contiguous(), off[1:].contiguous()
+    # mask chain buffers
+    m_ioff = torch.empty(n_lists + 1, dtype=torch.int64, device=dev)
+    m_idx = torch.empty(E, dtype=torch.int64, device=dev)
+    f_m2i(m_ioff.data_ptr(), m_idx.data_ptr(), mask.data_ptr(), off.data_ptr(), n_lists,
+          err.data_ptr(), sp)
+    Km = int(m_ioff[-1].item())
+    m_ist, m_isp = m_ioff[:-1].contiguous(), m_ioff[1:].contiguous()
+    m_too = torch.empty(n_lists + 1, dtype=torch.int64, device=dev)
+    m_carry = torch.empty(Km, dtype=torch.int64, device=dev)
+    m_out = torch.empty(Km, dtype=torch.float32, device=dev)
+
+    def mask_chain():
+        f_m2i(m_ioff.data_ptr(), m_idx.data_ptr(), mask.data_ptr(), off.data_ptr(), n_lists,
+              err.data_ptr(), sp)
+        k_apply(m_too, m_carry, m_ist, m_isp, n_lists, m_idx[:Km], Km, starts, stops, E)
+        f_take(m_out.data_ptr(), x.data_ptr(), 4, m_carry.data_ptr(), Km, E, 0, err.data_ptr(), sp)
+
+    Ki = idx.numel()
+    i_ist, i_isp = ioff[:-1].contiguous(), ioff[1:].contiguous()
+    i_too = torch.empty(n_lists + 1, dtype=torch.int64, device=dev)
+    i_carry = torch.empty(Ki, dtype=torch.int64, device=dev)
+    i_out = torch.empty(Ki, dtype=torch.float32, device=dev)
+
+    def index_chain():
+        k_apply(i_too, i_carry, i_ist, i_isp, n_lists, idx, Ki, starts, stops, E)
+        f_take(i_out.data_ptr(), x.data_ptr(), 4, i_carry.data_ptr(), Ki, E, 0, err.data_ptr(), sp)
+
+    Lo = torch.poisson(torch.full((n_lists,), 4.0, device=dev), generator=gen).to(torch.int64)
+    ninner = int(Lo.sum().item())
+    Li = torch.poisson(torch.full((ninner,), 6.0, device=dev), generator=gen).to(torch.int64)
+    inner = torch.zeros(ninner + 1, dtype=torch.int64, device=dev)
+    torch.cumsum(Li, 0, out=inner[1:])
+    E2 = int(inner[-1].item())
+    x2 = (torch.empty(E2, device=dev).exponential_(1.0, generator=gen) * 20).to(torch.float32)
+    in_st, in_sp = inner[:-1].contiguous(), inner[1:].contiguous()
+    k_cl = be["awkward_ListArray_getitem_next_range_carrylength", np.int64, np.int64, np.int64]
+    k_nr = be["awkward_ListArray_getitem_next_range", np.int64, np.int64, np.int64, np.int64]
+    cl = torch.empty(1, dtype=torch.int64, device=dev)
+    k_cl(cl, in_st, in_sp, ninner, 1, jagged.SLICE_NONE, 1)
+    be.synchronize()
+    Kr = int(cl.item())
+    r_off = torch.empty(ninner + 1, dtype=torch.int64, device=dev)
+    r_carry = torch.empty(Kr, dtype=torch.int64, device=dev)
+    r_out = torch.empty(Kr, dtype=torch.float32, device=dev)
+
+    def range_chain():
+        k_cl(cl, in_st, in_sp, ninner, 1, jagged.SLICE_NONE, 1)
+        k_nr(r_off, r_carry, in_st, in_sp, ninner, 1, jagged.SLICE_NONE, 1)
+        f_take(r_out.data_ptr(), x2.data_ptr(), 4, r_carry.data_ptr(), Kr, E2, 0, err.data_ptr(), sp)
+
+    res = {}
+    # algorithmic bytes: mask 1B/elem + offsets 8(N+1) read; index offsets 8(N+1) + index 8K
+    # written and read; apply 32N + 16K + 8(N+1); take 8K carry + 4K gather + 4K out
+    N = n_lists
+    byts = {
+        "mask": (E + 8 * (N + 1)) + (8 * (N + 1) + 8 * Km) + (32 * N + 16 * Km + 8 * (N + 1))
+        + 16 * Km,
+        "index": (32 * N + 16 * Ki + 8 * (N + 1)) + 16 * Ki,
+        "range": (16 * ninner + 8) + (16 * ninner + 8 * (ninner + 1) + 8 * Kr) + 16 * Kr,
+    }
+    for name, fn, nl in (("mask", mask_chain, N), ("index", index_chain, N),
+                         ("range", range_chain, N)):
+        for _ in range(max(warmup, 3)):
+            fn()
+        be.synchronize()
+        ms = _time_ms(fn, reps, stream)
+        be.synchronize()
+        res[name] = {"ms": round(ms, 4), "lists_per_s": round(nl / (ms * 1e-3), 1),
+                     "gbs": round(byts[name] / (ms * 1e-3) / 1e9, 1)}
+    res["mask"]["kernels"] = "mask_to_index + jagged_apply + take (float32)"
+    res["index"]["kernels"] = "jagged_apply + take (float32)"
+    res["range"]["kernels"] = "next_range_carrylength + next_range + take (float32)"
+    res["sizes"] = {"lists": N, "elements": E, "selected": Km, "indices": Ki,
+                    "inner_lists": ninner, "inner_elements": E2, "range_kept": Kr}
+    return res
+
+
+def measure_c4(dev, narrays=4096, min_lists=1_000, max_lists=20_000, reps=5):
+    """Batched uneven workload: sum/max/argmax/count(axis=-1) + array[mask] of
+    `narrays` float64 arrays, list counts log-uniform in [min_lists, max_lists]
+    (the [1e3, 2e6] range would hold ~270 GB of content; scaled to 2e4 at the
+    top), lengths Poisson(U(1,32)) or Geometric(0.02) per array, 5% empty.
+    Batched: one CUDA graph replay (autotuned plan).  Plain: the per-array
+    entry points array by array (wall time, host reads included)."""
+    import torch
+
+    from awkward_gb300 import batch
+
+    b = batch.make_batch(narrays, seed=4, min_lists=min_lists, max_lists=max_lists, device=dev)
+    variant = batch.autotune(b, reps=3)
+    plan = b.plan(*variant)
+    g = b.graph(plan)
+    g.replay()
+    torch.cuda.synchronize(dev)
+    stream = torch.cuda.current_stream(dev)
+    ms_batched = _time_ms(g.replay, reps, stream)
+    b.check_errors()
+    batch.run_plain(b)  # warm the per-array path (pools, kernel table)
+    ms_plain = batch.time_plain(b, reps=1)
+    E = int(b.nelements.sum())
+    N = int(b.nlists.sum())
+    byts = 3 * (8 * E + 16 * N) + (8 * E + E + 16 * N) + 8 * int(0.4 * E)
+    b.close()
+    return {"arrays": narrays, "lists": N, "elements": E, "plan": {"order_mode": variant[0],
+            "occupancy_div": variant[1]},
+            "batched_ms": round(ms_batched, 3), "plain_ms": round(ms_plain, 1),
+            "speedup": round(ms_plain / ms_batched, 1),
+            "batched_gbs": round(byts / (ms_batched * 1e-3) / 1e9, 1),
+            "list_counts": f"log-uniform [{min_lists}, {max_lists}]"}
+
+
+def measure_c5(dev, reps, warmup, n_lists=4_000_000):
+    """Differentiable ops at 4M lists, Poisson(16), float32: forward + backward
+    of segmented sum, max and jagged softmax (256 MB activation budget: the
+    softmax backward recomputes max and normaliser)."""
+    import torch
+
+    from awkward_gb300 import autograd as ag
+
+    gen = torch.Generator(device=dev).manual_seed(5)
+    L = torch.poisson(torch.full((n_lists,), 16.0, device=dev), generator=gen).to(torch.int64)
+    off = torch.zeros(n_lists + 1, dtype=torch.int64, device=dev)
+    torch.cumsum(L, 0, out=off[1:])
+    E = int(off[-1].item())
+    x = torch.randn(E, dtype=torch.float32, device=dev, generator=gen).requires_grad_(True)
+    stream = torch.cuda.current_stream(dev)
+    res = {}
+    for name, fn in (("sum", ag.segment_sum), ("max", ag.segment_max),
+                     ("softmax", ag.jagged_softmax)):
+        y = fn(x, off)
+        g = torch.randn(y.shape, dtype=torch.float32, device=dev, generator=gen)
+
+        def step():
+            x.grad = None
+            fn(x, off).backward(g)
+
+        for _ in range(max(warmup, 3)):
+            step()
+        torch.cuda.synchronize(dev)
+        ms = _time_ms(step, reps, stream)
+        res[name] = {"fwd_bwd_ms": round(ms, 4)}
+    res["sizes"] = {"lists": n_lists, "elements": E}
+    return res
+
+
 def run_gb300(args):
     import torch
 
@@ -309,6 +487,17 @@ def run_gb300(args):
     rank, world, local = dist_setup(args.gpus)
     dev = torch.device("cuda", torch.cuda.current_device())
     be = awkward_gb300.backend()
+    if args.only == "c2":
+        print(json.dumps({"c2_jagged_slicing": measure_c2(be, dev, args.steps, args.warmup,
+                                                          args.lists or 10_000_000)}))
+        return
+    if args.only == "c4":
+        print(json.dumps({"c4_batched": measure_c4(dev, narrays=args.lists or 4096)}))
+        return
+    if args.only == "c5":
+        print(json.dumps({"c5_autograd": measure_c5(dev, args.steps, args.warmup,
+                                                    args.lists or 4_000_000)}))
+        return
     if args.only == "c3":
         n2 = args.lists or 5_000_000
         print(json.dumps({"c3_combinations": measure_c3(be, dev, args.steps, args.warmup, n2,
@@ -439,6 +628,9 @@ def run_gb300(args):
     }
     if rank == 0 and not args.no_extras:
         line["c3_combinations"] = measure_c3(be, dev, max(args.steps // 2, 5), args.warmup)
+        line["c2_jagged_slicing"] = measure_c2(be, dev, max(args.steps // 2, 5), args.warmup)
+        line["c5_autograd"] = measure_c5(dev, max(args.steps // 2, 5), args.warmup)
+        line["c4_batched"] = measure_c4(dev)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(2_000_000, 1, 8.0).items()
                                 if k != "ms_per_step"}
@@ -459,7 +651,7 @@ def main():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the secondary workloads (combinations, ...)")
-    p.add_argument("--only", default=None, choices=["c3"],
+    p.add_argument("--only", default=None, choices=["c2", "c3", "c4", "c5"],
                    help="run one secondary workload alone (profiling); --lists sets its size")
     p.add_argument("--lists", type=int, default=None,
                    help="list count (default: 10M lists for the reducers, 5M for --only c3; "
