@@ -101,15 +101,30 @@ EXTENSIONS["awkward_gb300_batch_plan_create"] = (
 EXTENSIONS["awkward_gb300_batch_plan_run"] = ([("void*", "plan"), ("void*", "stream")], "batch")
 EXTENSIONS["awkward_gb300_batch_plan_destroy"] = ([("void*", "plan")], "batch")
 
+_PIPELINE_COMMENT = """host-buffer reduction with overlapped transfers (no counterpart in
+awkward): segmented sum, max (identity -inf) and argmax of a float64
+ListOffsetArray in pinned host memory.  Lists are cut into `chunks`
+(1..64) at list boundaries; copies in of chunk c+1, the reductions of
+chunk c and copies back of chunk c-1 overlap.  Device workspace: d_x
+(element j at d_x[j]), d_offsets [nlists + 1], three outputs [nlists].
+Returns after enqueueing; `stream` waits for the last copy back."""
+
+EXTENSIONS["awkward_gb300_reduce_sum_max_argmax_host_float64"] = (
+    [("double*", "h_sum"), ("double*", "h_max"), ("int64_t*", "h_argmax"),
+     ("const double*", "h_x"), ("const int64_t*", "h_offsets"), ("int64_t", "nlists"),
+     ("double*", "d_x"), ("int64_t*", "d_offsets"), ("double*", "d_sum"), ("double*", "d_max"),
+     ("int64_t*", "d_argmax"), ("int64_t", "chunks"), ("void*", "stream")], "pipeline")
+
 GROUP_COMMENTS = {"noalloc": _NOALLOC_COMMENT, "autograd": _AUTOGRAD_COMMENT,
-                  "jagged": _JAGGED_COMMENT, "batch": _BATCH_COMMENT}
+                  "jagged": _JAGGED_COMMENT, "batch": _BATCH_COMMENT,
+                  "pipeline": _PIPELINE_COMMENT}
 GROUP_DEFINES = {"noalloc": ["#define AWKWARD_GB300_NOALLOC_MAX_LISTS 67108864LL"]}
 
 
 def header_lines():
     """Declarations of the extension entry points, grouped, for the C header."""
     out = []
-    for group in ("noalloc", "jagged", "autograd", "batch"):
+    for group in ("noalloc", "jagged", "autograd", "batch", "pipeline"):
         out.append("")
         text = GROUP_COMMENTS[group].splitlines()
         out.append(f"/* ---- {text[0]}")

@@ -562,26 +562,20 @@ def run_gb300(args):
     step_bytes = 3 * algorithmic_bytes(n, e)
     value = world * step_bytes / (ms * 1e-3) / 1e9
 
-    # end to end through the C ABI from pinned host buffers
+    # end to end through the public host-buffer call (pinned host inputs and
+    # outputs; chunked transfers overlapped with the reductions)
+    from awkward_gb300 import pipeline
+
     x_pin = torch.from_numpy(x_h).pin_memory()
     off_pin = torch.from_numpy(off_h).pin_memory()
-    outs_pin = [torch.empty(n, dtype=torch.float64).pin_memory(),
+    outs_pin = (torch.empty(n, dtype=torch.float64).pin_memory(),
                 torch.empty(n, dtype=torch.float64).pin_memory(),
-                torch.empty(n, dtype=torch.int64).pin_memory()]
-    xd = torch.empty_like(x)
-    offd = torch.empty_like(off)
-    startsd = torch.empty_like(starts)
+                torch.empty(n, dtype=torch.int64).pin_memory())
+    ws = pipeline.Workspace(n, int(off_h[-1]), device=dev)
+    del x, off, starts  # the workspace holds the device copies
 
     def e2e_step():
-        xd.copy_(x_pin, non_blocking=True)
-        offd.copy_(off_pin, non_blocking=True)
-        startsd.copy_(offd[:-1])
-        k_sum(o_sum, xd, offd, n)
-        k_max(o_max, xd, offd, n, -np.inf)
-        k_arg(o_arg, xd, offd, startsd, n)
-        outs_pin[0].copy_(o_sum, non_blocking=True)
-        outs_pin[1].copy_(o_max, non_blocking=True)
-        outs_pin[2].copy_(o_arg, non_blocking=True)
+        pipeline.reduce_host(x_pin, off_pin, chunks=args.chunks, workspace=ws, out=outs_pin)
 
     for _ in range(2):
         e2e_step()
@@ -598,7 +592,6 @@ def run_gb300(args):
     ms_e2e = reduce_max(s2.elapsed_time(t2) / args.steps)
     e2e_value = world * step_bytes / (ms_e2e * 1e-3) / 1e9
 
-    # parity spot check of the timed outputs against the oracle on a slice
     dominant = max(per, key=per.get)
     peak, peak_kind = measured_peak()
     achieved = algorithmic_bytes(n, e) / (per[dominant] * 1e-3) / 1e9
@@ -622,7 +615,8 @@ def run_gb300(args):
                      "algorithmic_bytes_per_launch": algorithmic_bytes(n, e)},
         "e2e": {"value": round(e2e_value, 2), "unit": UNIT,
                 "h2d_bytes_per_step": int(8 * e + 8 * (n + 1)),
-                "d2h_bytes_per_step": int(3 * 8 * n), "ms_per_step": round(ms_e2e, 4)},
+                "d2h_bytes_per_step": int(3 * 8 * n), "ms_per_step": round(ms_e2e, 4),
+                "path": f"awkward_gb300.pipeline.reduce_host, {args.chunks} chunks"},
         "gpu_launches": args.steps * 3 * 2,
         "clocks": sampler.summary(),
     }
@@ -649,6 +643,8 @@ def main():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--chunks", type=int, default=8,
+                   help="list chunks of the host-buffer (e2e) pipeline")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the secondary workloads (combinations, ...)")
     p.add_argument("--only", default=None, choices=["c2", "c3", "c4", "c5"],

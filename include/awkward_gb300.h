@@ -494,6 +494,15 @@ int awkward_gb300_batch_plan_create(void** plan, int64_t narrays, const int64_t*
 int awkward_gb300_batch_plan_run(void* plan, void* stream);
 int awkward_gb300_batch_plan_destroy(void* plan);
 
+/* ---- host-buffer reduction with overlapped transfers (no counterpart in
+ * awkward): segmented sum, max (identity -inf) and argmax of a float64
+ * ListOffsetArray in pinned host memory.  Lists are cut into `chunks`
+ * (1..64) at list boundaries; copies in of chunk c+1, the reductions of
+ * chunk c and copies back of chunk c-1 overlap.  Device workspace: d_x
+ * (element j at d_x[j]), d_offsets [nlists + 1], three outputs [nlists].
+ * Returns after enqueueing; `stream` waits for the last copy back. */
+int awkward_gb300_reduce_sum_max_argmax_host_float64(double* h_sum, double* h_max, int64_t* h_argmax, const double* h_x, const int64_t* h_offsets, int64_t nlists, double* d_x, int64_t* d_offsets, double* d_sum, double* d_max, int64_t* d_argmax, int64_t chunks, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
