@@ -495,11 +495,34 @@ __device__ __forceinline__ FxAcc run_short(const FixedSumOp<IN>& op, const IN* p
     return a;
   } else {
     const long long* q = reinterpret_cast<const long long*>(p);
-    int emax = 1, special = 0;
+    // pass 1 on the high words only: largest and smallest exponent field
+    const int* qh = reinterpret_cast<const int*>(p) + 1;
+    int ebmax = 0, ebmin = 0x7ff00000;
     for (int i = 0; i < n; i++) {
-      const int e = (int)((unsigned long long)__ldg(q + i) >> 52) & 0x7ff;
-      emax = e > emax ? e : emax;
+      const int eb = __ldg(qh + 2 * i) & 0x7ff00000;
+      ebmax = eb > ebmax ? eb : ebmax;
+      ebmin = eb < ebmin ? eb : ebmin;
     }
+    const int emax_f = ebmax >> 20, emin_f = ebmin >> 20;
+    if (n > 0 && emax_f != 0x7ff && emin_f != 0 && emax_f - emin_f < 32) {
+      // every element normal and within 32 binades of the largest: the
+      // aligned significand is two funnel shifts (same bits as below)
+      long long acc = 0;
+      for (int i = 0; i < n; i++) {
+        const long long b = __ldg(q + i);
+        const unsigned hi = (unsigned)((unsigned long long)b >> 32);
+        const unsigned d = (unsigned)(emax_f - (int)((hi >> 20) & 0x7ff));
+        const unsigned mh = (hi & 0xfffffu) | 0x100000u;
+        const unsigned ml = (unsigned)b;
+        const unsigned tl = __funnelshift_r(ml, mh, d);
+        const unsigned th = mh >> d;
+        const long long t = (long long)(((unsigned long long)th << 32) | tl);
+        const long long sg = b >> 63;
+        acc += (t ^ sg) - sg;
+      }
+      return FxAcc{acc, emax_f, 0};
+    }
+    int emax = emax_f > 1 ? emax_f : 1, special = 0;
     special = emax == 0x7ff;
     if (special) {  // inf / NaN present: the general path tracks them
       FxAcc a = op.identity();

@@ -80,9 +80,10 @@ __device__ __forceinline__ long long mp_search_half(const int64_t* __restrict__ 
   long long hi = d < nlists ? d : nlists;  // answer in [lo, hi]
   auto pred = [&](long long k) { return (k + (__ldg(offsets + k + 1) - e0)) < d; };
   if (hi - lo > 16) {
-    // proportional guess g; probe g + (hl - 8) * w
+    // proportional guess g (float32: only a starting point, the probes that
+    // follow are exact); probe g + (hl - 8) * w
     const long long D = nlists + E;
-    long long g = D > 0 ? (long long)((double)d * (double)nlists / (double)D) : lo;
+    long long g = D > 0 ? (long long)((float)d * ((float)nlists / (float)D)) : lo;
     const long long w = ((hi - lo) >> 12) + 1;
     long long k = g + (long long)(hl - 8) * w;
     k = k < lo ? lo : (k > hi - 1 ? hi - 1 : k);
