@@ -158,9 +158,10 @@ __device__ __forceinline__ double fx_finalize(FxAcc a) {
       (long long)(sign | ((unsigned long long)biased << 52) | (q & 0xfffffffffffffULL)));
 }
 
-// Sum of float64 (or float32) into float64: exact on the integer pipe, then
-// rounded once (the CPU rounds after every addition; both are within
-// n*eps*sum|x| of the exact sum).
+// Sum of float64 (or float32) into float64 on the integer pipe in fixed
+// point, rounded once at the end (runs of at most 32 elements also add half
+// their elements in float64, see run_short); within n*eps*sum|x| of the exact
+// sum, like the CPU loop that rounds after every addition.
 template <class IN>
 struct FixedSumOp {
   using In = IN;
@@ -494,52 +495,59 @@ __device__ __forceinline__ FxAcc run_short(const FixedSumOp<IN>& op, const IN* p
     for (int i = 0; i < n; i++) a = op.step(a, __ldg(p + i), 0, false, 0);
     return a;
   } else {
+    // Even positions are added in float64 (one DADD per pair, on the FP64
+    // unit, which otherwise idles) while odd positions go through the exact
+    // fixed point on the integer pipes; the double partial joins the fixed
+    // point once (fx_add_f64 also carries its inf/NaN).  The result stays
+    // within n*eps*sum|x| of the exact sum.
     const long long* q = reinterpret_cast<const long long*>(p);
-    // pass 1 on the high words only: largest and smallest exponent field
     const int* qh = reinterpret_cast<const int*>(p) + 1;
+    double dsum = 0.0;
     int ebmax = 0, ebmin = 0x7ff00000;
-    for (int i = 0; i < n; i++) {
-      const int eb = __ldg(qh + 2 * i) & 0x7ff00000;
+    int i = 0;
+    for (; i + 1 < n; i += 2) {
+      dsum += __ldg(p + i);
+      const int eb = __ldg(qh + 2 * (i + 1)) & 0x7ff00000;
       ebmax = eb > ebmax ? eb : ebmax;
       ebmin = eb < ebmin ? eb : ebmin;
     }
+    if (i < n) dsum += __ldg(p + i);
+    const int half = n >> 1;  // odd positions 1, 3, ..., 2*half-1
+    if (half == 0) return fx_add_f64(op.identity(), dsum);
     const int emax_f = ebmax >> 20, emin_f = ebmin >> 20;
-    if (n > 0 && emax_f != 0x7ff && emin_f != 0 && emax_f - emin_f < 32) {
-      // every element normal and within 32 binades of the largest: the
-      // aligned significand is two funnel shifts (same bits as below)
-      long long acc = 0;
-      for (int i = 0; i < n; i++) {
-        const long long b = __ldg(q + i);
+    long long acc = 0;
+    int anchor;
+    if (emax_f != 0x7ff && emin_f != 0 && emax_f - emin_f < 32) {
+      // every odd element normal and within 32 binades: two funnel shifts each
+      for (int k = 1; k < n; k += 2) {
+        const long long b = __ldg(q + k);
         const unsigned hi = (unsigned)((unsigned long long)b >> 32);
         const unsigned d = (unsigned)(emax_f - (int)((hi >> 20) & 0x7ff));
         const unsigned mh = (hi & 0xfffffu) | 0x100000u;
-        const unsigned ml = (unsigned)b;
-        const unsigned tl = __funnelshift_r(ml, mh, d);
+        const unsigned tl = __funnelshift_r((unsigned)b, mh, d);
         const unsigned th = mh >> d;
         const long long t = (long long)(((unsigned long long)th << 32) | tl);
         const long long sg = b >> 63;
         acc += (t ^ sg) - sg;
       }
-      return FxAcc{acc, emax_f, 0};
-    }
-    int emax = emax_f > 1 ? emax_f : 1, special = 0;
-    special = emax == 0x7ff;
-    if (special) {  // inf / NaN present: the general path tracks them
+      anchor = emax_f;
+    } else if (emax_f == 0x7ff) {  // inf / NaN among them: the general accumulator
       FxAcc a = op.identity();
-      for (int i = 0; i < n; i++) a = fx_add_f64(a, __longlong_as_double(__ldg(q + i)));
-      return a;
+      for (int k = 1; k < n; k += 2) a = fx_add_f64(a, __longlong_as_double(__ldg(q + k)));
+      return fx_add_f64(a, dsum);
+    } else {  // zeros, subnormals or a wide exponent spread
+      anchor = emax_f > 1 ? emax_f : 1;
+      for (int k = 1; k < n; k += 2) {
+        const long long b = __ldg(q + k);
+        const int e = (int)((unsigned long long)b >> 52) & 0x7ff;
+        const long long m = (b & 0xfffffffffffffLL) | ((long long)(e != 0) << 52);
+        const int d = anchor - (e ? e : 1);
+        const long long t = m >> (d < 63 ? d : 63);
+        const long long sg = b >> 63;  // 0 or -1
+        acc += (t ^ sg) - sg;
+      }
     }
-    long long acc = 0;
-    for (int i = 0; i < n; i++) {
-      const long long b = __ldg(q + i);
-      const int e = (int)((unsigned long long)b >> 52) & 0x7ff;
-      const long long m = (b & 0xfffffffffffffLL) | ((long long)(e != 0) << 52);
-      const int d = emax - (e ? e : 1);
-      const long long t = m >> (d < 63 ? d : 63);
-      const long long sg = b >> 63;  // 0 or -1
-      acc += (t ^ sg) - sg;
-    }
-    return FxAcc{acc, emax, 0};
+    return fx_add_f64(FxAcc{acc, anchor, 0}, dsum);
   }
 }
 
