@@ -551,6 +551,131 @@ __device__ __forceinline__ FxAcc run_short(const FixedSumOp<IN>& op, const IN* p
   }
 }
 
+// ---------------------------------------------------------------- warp runs
+// Reduce elements [s, e) of list `li` (first element st) with the whole warp,
+// lanes strided (coalesced loads); every lane returns the result.  The
+// default steps the op element by element and combines across lanes.
+template <class Op>
+__device__ __forceinline__ typename Op::Acc run_coop_exact(const Op& op,
+                                                           const store_t<typename Op::In>* x,
+                                                           long long s, long long e, long long st,
+                                                           long long li) {
+  const int lane = threadIdx.x & 31;
+  typename Op::Acc a = op.identity();
+  for (long long j = s + lane; j < e; j += 32) a = op.step(a, __ldg(x + j), j, j == st, li);
+  return warp_allreduce(op, a);
+}
+
+template <class Op>
+__device__ __forceinline__ typename Op::Acc run_coop(const Op& op,
+                                                     const store_t<typename Op::In>* x,
+                                                     long long s, long long e, long long st,
+                                                     long long li) {
+  return run_coop_exact(op, x, s, e, st, li);
+}
+
+// Float64 sum: a warp-wide largest exponent, then every lane adds its
+// elements aligned to it (one anchor: no renormalisation inside the run, the
+// same truncation whatever the lane order) and the lanes' fixed-point
+// partials are combined.  Runs with an infinity or NaN, or longer than 8192
+// elements (a lane partial could exceed 2^62), take the general accumulator.
+template <class IN>
+__device__ __forceinline__ FxAcc run_coop(const FixedSumOp<IN>& op, const IN* x, long long s,
+                                          long long e, long long st, long long li) {
+  if constexpr (!std::is_same<IN, double>::value) {
+    return run_coop_exact(op, x, s, e, st, li);
+  } else {
+    if (e - s > 8192) return run_coop_exact(op, x, s, e, st, li);
+    const int lane = threadIdx.x & 31;
+    const int* xh = reinterpret_cast<const int*>(x) + 1;
+    int eb = 0;
+    for (long long j = s + lane; j < e; j += 32) {
+      const int v = __ldg(xh + 2 * j) & 0x7ff00000;
+      eb = v > eb ? v : eb;
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) {
+      const int o = __shfl_xor_sync(0xffffffffu, eb, d);
+      eb = o > eb ? o : eb;
+    }
+    const int emax_f = eb >> 20;
+    if (emax_f == 0x7ff) return run_coop_exact(op, x, s, e, st, li);
+    const int anchor = emax_f > 1 ? emax_f : 1;
+    const long long* q = reinterpret_cast<const long long*>(x);
+    long long acc = 0;
+    for (long long j = s + lane; j < e; j += 32) {
+      const long long b = __ldg(q + j);
+      const int ex = (int)((unsigned long long)b >> 52) & 0x7ff;
+      const long long m = (b & 0xfffffffffffffLL) | ((long long)(ex != 0) << 52);
+      const int d = anchor - (ex ? ex : 1);
+      const long long t = m >> (d < 63 ? d : 63);
+      const long long sg = b >> 63;
+      acc += (t ^ sg) - sg;
+    }
+    return warp_allreduce(op, FxAcc{acc, anchor, 0});
+  }
+}
+
+// Float64 extrema: lanes reduce raw order keys (first occurrence kept by the
+// strict comparison, ties across lanes to the lower index); the result is the
+// exact op's unless the winner is a zero or a NaN, or (argmax/argmin) the run
+// starts the list with a NaN -- then the run is redone exactly.
+// (runs shorter than 2^30; positions kept as 32-bit offsets from s)
+template <bool MAX>
+__device__ __forceinline__ void raw_warp_best(const double* x, long long s, long long e,
+                                              long long* rk, long long* idx) {
+  const int lane = threadIdx.x & 31;
+  const long long* q = reinterpret_cast<const long long*>(x + s);
+  const int n = (int)(e - s);
+  long long best = kKeyLow;
+  int at = -1;
+  for (int j = lane; j < n; j += 32) {
+    const long long k = MAX ? f64_raw_key(__ldg(q + j)) : ~f64_raw_key(__ldg(q + j));
+    if (at < 0 || k > best) {
+      best = k;
+      at = j;
+    }
+  }
+#pragma unroll
+  for (int d = 16; d > 0; d >>= 1) {
+    const long long ob = __shfl_xor_sync(0xffffffffu, best, d);
+    const int oa = __shfl_xor_sync(0xffffffffu, at, d);
+    const bool take = oa >= 0 && (at < 0 || ob > best || (ob == best && oa < at));
+    best = take ? ob : best;
+    at = take ? oa : at;
+  }
+  *rk = best;
+  *idx = at < 0 ? -1 : s + at;
+}
+
+template <bool MAX>
+__device__ __forceinline__ typename ExtremumOp<double, MAX>::Acc run_coop(
+    const ExtremumOp<double, MAX>& op, const double* x, long long s, long long e, long long st,
+    long long li) {
+  if (e - s >= (1ll << 30)) return run_coop_exact(op, x, s, e, st, li);
+  long long rk, at;
+  raw_warp_best<MAX>(x, s, e, &rk, &at);
+  if (at < 0) return op.identity();
+  const long long bits = __ldg(reinterpret_cast<const long long*>(x) + at);
+  if (raw_key_exact(f64_raw_key(bits))) return {f64_dir_key<MAX>(__longlong_as_double(bits)), bits, at};
+  return run_coop_exact(op, x, s, e, st, li);
+}
+
+template <bool MAX>
+__device__ __forceinline__ typename ArgExtremumOp<double, MAX>::Acc run_coop(
+    const ArgExtremumOp<double, MAX>& op, const double* x, long long s, long long e, long long st,
+    long long li) {
+  if (e - s >= (1ll << 30)) return run_coop_exact(op, x, s, e, st, li);
+  long long rk, at;
+  raw_warp_best<MAX>(x, s, e, &rk, &at);
+  if (at < 0) return op.identity();
+  const long long bits = __ldg(reinterpret_cast<const long long*>(x) + at);
+  const bool lead_nan = st >= s && st < e && is_nan(__ldg(x + st));
+  if (raw_key_exact(f64_raw_key(bits)) && !lead_nan)
+    return {f64_dir_key<MAX>(__longlong_as_double(bits)), at};
+  return run_coop_exact(op, x, s, e, st, li);
+}
+
 template <class IN>
 struct SumSqOp {
   using In = IN;

@@ -179,9 +179,7 @@ __device__ __forceinline__ void seg_reduce_range(const Op& op,
       const long long e2 = __shfl_sync(0xffffffffu, e, src);
       const long long st2 = __shfl_sync(0xffffffffu, st, src);
       const long long l2 = base + src;
-      typename Op::Acc a2 = op.identity();
-      for (long long j = s2 + lane; j < e2; j += 32) a2 = op.step(a2, ld_ro(x + j), j, j == st2, l2);
-      a2 = warp_allreduce(op, a2);
+      const typename Op::Acc a2 = run_coop(op, x, s2, e2, st2, l2);
       if (lane == src) acc = a2;
     }
     if (act && !skip) {
