@@ -164,6 +164,41 @@ __global__ void __launch_bounds__(kTileBlock)
   // walking forward from the list of the step's first slot.
   constexpr int kWarps = kTileBlock / 32;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (n == 2 && total < (1ll << 31)) {
+    // pairs of a tile with fewer than 2^31 of them: tile-local positions in 32 bits
+    __shared__ int loc32[kTileLists + 1];
+    for (int i = threadIdx.x; i <= kTileLists; i += kTileBlock) loc32[i] = (int)sm.loc[i];
+    __syncthreads();
+    const int t32 = (int)total;
+    const int qa = (int)((long long)t32 * warp / kWarps), qb = (int)((long long)t32 * (warp + 1) / kWarps);
+    if (qa >= qb) return;
+    int64_t* __restrict__ out0 = s_ptr[0];
+    int64_t* __restrict__ out1 = s_ptr[1];
+    const int shift = replacement ? 1 : 0;
+    int r = tile_find(sm, qa);
+    for (int g = qa; g < qb; g += 32) {
+      while (loc32[r + 1] <= g) r++;
+      const int q = g + lane;
+      if (q >= qb) continue;
+      int rl = r;
+      while (loc32[rl + 1] <= q) rl++;
+      const int rank = q - loc32[rl];
+      const long long s = s_size[rl];
+      const long long base = s_start[rl];
+      long long a, b;
+      if (s < (1ll << 15)) {
+        int ai, bi;
+        unrank2_small((int)s, rank, &ai, &bi);
+        a = ai;
+        b = bi;
+      } else {
+        unrank2(s, rank, &a, &b);
+      }
+      out0[prefix + q] = base + a;
+      out1[prefix + q] = base + b - shift;
+    }
+    return;
+  }
   const long long qa = total * warp / kWarps, qb = total * (warp + 1) / kWarps;
   if (qa >= qb) return;
   int r = tile_find(sm, qa);
