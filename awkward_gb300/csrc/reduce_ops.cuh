@@ -552,58 +552,77 @@ __device__ __forceinline__ FxAcc run_short(const FixedSumOp<IN>& op, const IN* p
 }
 
 // ---------------------------------------------------------------- warp runs
-// Reduce elements [s, e) of list `li` (first element st) with the whole warp,
-// lanes strided (coalesced loads); every lane returns the result.  The
-// default steps the op element by element and combines across lanes.
-template <class Op>
+// Reduce elements [s, e) of list `li` (first element st) with a group of G
+// lanes (G = 32: the whole warp; G = 8: four groups, four lists at once),
+// lanes strided within the group; every lane of the group returns the
+// result.  All lanes of the warp call together (every group with its own
+// list); any fallback to the exact path is taken by the whole warp.
+
+// Combine across the G lanes of a group.
+template <int G, class Op>
+__device__ __forceinline__ typename Op::Acc group_allreduce(const Op& op, typename Op::Acc a) {
+#pragma unroll
+  for (int d = G / 2; d > 0; d >>= 1) {
+    constexpr int W = sizeof(typename Op::Acc) / 4;
+    union U { typename Op::Acc v; uint32_t w[W]; } u;
+    u.v = a;
+#pragma unroll
+    for (int i = 0; i < W; i++) u.w[i] = __shfl_xor_sync(0xffffffffu, u.w[i], d);
+    a = op.combine(a, u.v);
+  }
+  return a;
+}
+
+template <int G, class Op>
 __device__ __forceinline__ typename Op::Acc run_coop_exact(const Op& op,
                                                            const store_t<typename Op::In>* x,
                                                            long long s, long long e, long long st,
                                                            long long li) {
-  const int lane = threadIdx.x & 31;
+  const int sub = threadIdx.x & (G - 1);
   typename Op::Acc a = op.identity();
-  for (long long j = s + lane; j < e; j += 32) a = op.step(a, __ldg(x + j), j, j == st, li);
-  return warp_allreduce(op, a);
+  for (long long j = s + sub; j < e; j += G) a = op.step(a, __ldg(x + j), j, j == st, li);
+  return group_allreduce<G>(op, a);
 }
 
-template <class Op>
-__device__ __forceinline__ typename Op::Acc run_coop(const Op& op,
-                                                     const store_t<typename Op::In>* x,
-                                                     long long s, long long e, long long st,
-                                                     long long li) {
-  return run_coop_exact(op, x, s, e, st, li);
+template <int G, class Op>
+__device__ typename Op::Acc run_coop(const Op& op, const store_t<typename Op::In>* x, long long s,
+                                     long long e, long long st, long long li) {
+  return run_coop_exact<G>(op, x, s, e, st, li);
 }
 
-// Float64 sum: a warp-wide largest exponent, then every lane adds its
+// Float64 sum: a group-wide largest exponent, then every lane adds its
 // elements aligned to it (one anchor: no renormalisation inside the run, the
 // same truncation whatever the lane order) and the lanes' fixed-point
-// partials are combined.  Runs with an infinity or NaN, or longer than 8192
-// elements (a lane partial could exceed 2^62), take the general accumulator.
-template <class IN>
-__device__ __forceinline__ FxAcc run_coop(const FixedSumOp<IN>& op, const IN* x, long long s,
-                                          long long e, long long st, long long li) {
+// partials are combined.  Runs with an infinity or NaN, or with more than 256
+// elements per lane (a lane partial could exceed 2^62), take the general
+// accumulator.
+template <int G, class IN>
+__device__ __forceinline__ FxAcc run_coop_sum(const FixedSumOp<IN>& op, const IN* x, long long s,
+                                              long long e, long long st, long long li) {
   if constexpr (!std::is_same<IN, double>::value) {
-    return run_coop_exact(op, x, s, e, st, li);
+    return run_coop_exact<G>(op, x, s, e, st, li);
   } else {
-    if (e - s > 8192) return run_coop_exact(op, x, s, e, st, li);
-    const int lane = threadIdx.x & 31;
+    const int sub = threadIdx.x & (G - 1);
     const int* xh = reinterpret_cast<const int*>(x) + 1;
     int eb = 0;
-    for (long long j = s + lane; j < e; j += 32) {
-      const int v = __ldg(xh + 2 * j) & 0x7ff00000;
-      eb = v > eb ? v : eb;
-    }
+    const bool too_long = e - s > 256ll * G;
+    if (!too_long)
+      for (long long j = s + sub; j < e; j += G) {
+        const int v = __ldg(xh + 2 * j) & 0x7ff00000;
+        eb = v > eb ? v : eb;
+      }
 #pragma unroll
-    for (int d = 16; d > 0; d >>= 1) {
+    for (int d = G / 2; d > 0; d >>= 1) {
       const int o = __shfl_xor_sync(0xffffffffu, eb, d);
       eb = o > eb ? o : eb;
     }
     const int emax_f = eb >> 20;
-    if (emax_f == 0x7ff) return run_coop_exact(op, x, s, e, st, li);
+    if (__any_sync(0xffffffffu, too_long || emax_f == 0x7ff))
+      return run_coop_exact<G>(op, x, s, e, st, li);
     const int anchor = emax_f > 1 ? emax_f : 1;
     const long long* q = reinterpret_cast<const long long*>(x);
     long long acc = 0;
-    for (long long j = s + lane; j < e; j += 32) {
+    for (long long j = s + sub; j < e; j += G) {
       const long long b = __ldg(q + j);
       const int ex = (int)((unsigned long long)b >> 52) & 0x7ff;
       const long long m = (b & 0xfffffffffffffLL) | ((long long)(ex != 0) << 52);
@@ -612,24 +631,29 @@ __device__ __forceinline__ FxAcc run_coop(const FixedSumOp<IN>& op, const IN* x,
       const long long sg = b >> 63;
       acc += (t ^ sg) - sg;
     }
-    return warp_allreduce(op, FxAcc{acc, anchor, 0});
+    return group_allreduce<G>(op, FxAcc{acc, anchor, 0});
   }
+}
+template <int G, class IN>
+__device__ __forceinline__ FxAcc run_coop(const FixedSumOp<IN>& op, const IN* x, long long s,
+                                          long long e, long long st, long long li) {
+  return run_coop_sum<G>(op, x, s, e, st, li);
 }
 
 // Float64 extrema: lanes reduce raw order keys (first occurrence kept by the
 // strict comparison, ties across lanes to the lower index); the result is the
 // exact op's unless the winner is a zero or a NaN, or (argmax/argmin) the run
-// starts the list with a NaN -- then the run is redone exactly.
-// (runs shorter than 2^30; positions kept as 32-bit offsets from s)
-template <bool MAX>
-__device__ __forceinline__ void raw_warp_best(const double* x, long long s, long long e,
-                                              long long* rk, long long* idx) {
-  const int lane = threadIdx.x & 31;
+// starts the list with a NaN -- then the run is redone exactly.  Positions
+// are kept as 32-bit offsets from s (runs shorter than 2^30).
+template <int G, bool MAX>
+__device__ __forceinline__ void raw_group_best(const double* x, long long s, long long e,
+                                               long long* rk, long long* idx) {
+  const int sub = threadIdx.x & (G - 1);
   const long long* q = reinterpret_cast<const long long*>(x + s);
   const int n = (int)(e - s);
   long long best = kKeyLow;
   int at = -1;
-  for (int j = lane; j < n; j += 32) {
+  for (int j = sub; j < n; j += G) {
     const long long k = MAX ? f64_raw_key(__ldg(q + j)) : ~f64_raw_key(__ldg(q + j));
     if (at < 0 || k > best) {
       best = k;
@@ -637,7 +661,7 @@ __device__ __forceinline__ void raw_warp_best(const double* x, long long s, long
     }
   }
 #pragma unroll
-  for (int d = 16; d > 0; d >>= 1) {
+  for (int d = G / 2; d > 0; d >>= 1) {
     const long long ob = __shfl_xor_sync(0xffffffffu, best, d);
     const int oa = __shfl_xor_sync(0xffffffffu, at, d);
     const bool take = oa >= 0 && (at < 0 || ob > best || (ob == best && oa < at));
@@ -648,32 +672,40 @@ __device__ __forceinline__ void raw_warp_best(const double* x, long long s, long
   *idx = at < 0 ? -1 : s + at;
 }
 
-template <bool MAX>
+template <int G, bool MAX>
 __device__ __forceinline__ typename ExtremumOp<double, MAX>::Acc run_coop(
     const ExtremumOp<double, MAX>& op, const double* x, long long s, long long e, long long st,
     long long li) {
-  if (e - s >= (1ll << 30)) return run_coop_exact(op, x, s, e, st, li);
-  long long rk, at;
-  raw_warp_best<MAX>(x, s, e, &rk, &at);
+  const bool too_long = e - s >= (1ll << 30);
+  long long rk = kKeyLow, at = -1;
+  if (!__any_sync(0xffffffffu, too_long)) raw_group_best<G, MAX>(x, s, e, &rk, &at);
+  long long bits = 0;
+  bool exact = !too_long;
+  if (exact && at >= 0) {
+    bits = __ldg(reinterpret_cast<const long long*>(x) + at);
+    exact = raw_key_exact(f64_raw_key(bits));
+  }
+  if (__any_sync(0xffffffffu, !exact)) return run_coop_exact<G>(op, x, s, e, st, li);
   if (at < 0) return op.identity();
-  const long long bits = __ldg(reinterpret_cast<const long long*>(x) + at);
-  if (raw_key_exact(f64_raw_key(bits))) return {f64_dir_key<MAX>(__longlong_as_double(bits)), bits, at};
-  return run_coop_exact(op, x, s, e, st, li);
+  return {f64_dir_key<MAX>(__longlong_as_double(bits)), bits, at};
 }
 
-template <bool MAX>
+template <int G, bool MAX>
 __device__ __forceinline__ typename ArgExtremumOp<double, MAX>::Acc run_coop(
     const ArgExtremumOp<double, MAX>& op, const double* x, long long s, long long e, long long st,
     long long li) {
-  if (e - s >= (1ll << 30)) return run_coop_exact(op, x, s, e, st, li);
-  long long rk, at;
-  raw_warp_best<MAX>(x, s, e, &rk, &at);
+  const bool too_long = e - s >= (1ll << 30);
+  long long rk = kKeyLow, at = -1;
+  if (!__any_sync(0xffffffffu, too_long)) raw_group_best<G, MAX>(x, s, e, &rk, &at);
+  long long bits = 0;
+  bool exact = !too_long && !(st >= s && st < e && is_nan(__ldg(x + st)));
+  if (exact && at >= 0) {
+    bits = __ldg(reinterpret_cast<const long long*>(x) + at);
+    exact = raw_key_exact(f64_raw_key(bits));
+  }
+  if (__any_sync(0xffffffffu, !exact)) return run_coop_exact<G>(op, x, s, e, st, li);
   if (at < 0) return op.identity();
-  const long long bits = __ldg(reinterpret_cast<const long long*>(x) + at);
-  const bool lead_nan = st >= s && st < e && is_nan(__ldg(x + st));
-  if (raw_key_exact(f64_raw_key(bits)) && !lead_nan)
-    return {f64_dir_key<MAX>(__longlong_as_double(bits)), at};
-  return run_coop_exact(op, x, s, e, st, li);
+  return {f64_dir_key<MAX>(__longlong_as_double(bits)), at};
 }
 
 template <class IN>

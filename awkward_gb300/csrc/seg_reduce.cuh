@@ -64,6 +64,7 @@ struct RangeRecord {
 constexpr int kSegBlock = 256;        // threads per CTA (8 warps)
 constexpr int kSegMinBlocks = 5;      // resident CTAs per SM (40 warps of loads in flight)
 constexpr int kShortList = 32;        // longest list reduced by one lane
+constexpr int kMediumList = 256;      // longest list reduced by a group of 8 lanes
 constexpr int kMinRangeItems = 512;   // smallest merge range given to a warp
 constexpr long long kAbsorb = 4096;   // longest list reduced whole by the range where it ends
 
@@ -135,6 +136,12 @@ __device__ __forceinline__ T ld_ro(const T* p) {
   return __ldg(p);
 }
 
+// Reduction of one run of a list by a group of G lanes (defined, with its
+// per-reducer overloads, in reduce_ops.cuh).
+template <int G, class Op>
+__device__ typename Op::Acc run_coop(const Op& op, const store_t<typename Op::In>* x, long long s,
+                                     long long e, long long st, long long li);
+
 // Reduce the lists of merge-path diagonal range [d0, d1) of one array
 // (whole warp).  emit(list, acc) delivers each list reduced entirely here;
 // the partials of lists crossing the range ends go to `rec`.
@@ -171,7 +178,32 @@ __device__ __forceinline__ void seg_reduce_range(const Op& op,
     }
     typename Op::Acc acc = op.identity();
     if (act && !skip && e - s0 <= kShortList) acc = run_short(op, x + s0, (int)(e - s0), s0, st, li);
-    unsigned coop = __ballot_sync(0xffffffffu, act && !skip && e - s0 > kShortList);
+    const bool longer = act && !skip && e - s0 > kShortList;
+    // medium lists: four at a time, 8 lanes each (four load chains in flight)
+    unsigned med = __ballot_sync(0xffffffffu, longer && e - s0 <= kMediumList);
+    unsigned coop = __ballot_sync(0xffffffffu, longer) & ~med;
+    while (med) {
+      int src = -1;  // the list of this lane's group
+#pragma unroll
+      for (int g = 0; g < 4; g++) {
+        const int cand = med ? __ffs(med) - 1 : -1;
+        if (cand >= 0) med &= med - 1;
+        if ((lane >> 3) == g) src = cand;
+      }
+      const int from = src < 0 ? 0 : src;
+      long long s2 = __shfl_sync(0xffffffffu, s0, from);
+      long long e2 = __shfl_sync(0xffffffffu, e, from);
+      const long long st2 = __shfl_sync(0xffffffffu, st, from);
+      if (src < 0) e2 = s2;  // an idle group reduces nothing
+      const typename Op::Acc a2 = run_coop<8>(op, x, s2, e2, st2, base + from);
+      // the owner lane takes its list's result from the first lane of its group
+      int owner_group = -1;
+#pragma unroll
+      for (int g = 0; g < 4; g++)
+        if (__shfl_sync(0xffffffffu, src, g * 8) == lane) owner_group = g;
+      const typename Op::Acc mine = shfl_idx(a2, owner_group < 0 ? 0 : owner_group * 8);
+      if (owner_group >= 0) acc = mine;
+    }
     while (coop) {  // longer lists: the whole warp, strided (coalesced)
       const int src = __ffs(coop) - 1;
       coop &= coop - 1;
@@ -179,7 +211,7 @@ __device__ __forceinline__ void seg_reduce_range(const Op& op,
       const long long e2 = __shfl_sync(0xffffffffu, e, src);
       const long long st2 = __shfl_sync(0xffffffffu, st, src);
       const long long l2 = base + src;
-      const typename Op::Acc a2 = run_coop(op, x, s2, e2, st2, l2);
+      const typename Op::Acc a2 = run_coop<32>(op, x, s2, e2, st2, l2);
       if (lane == src) acc = a2;
     }
     if (act && !skip) {
