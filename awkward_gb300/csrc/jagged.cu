@@ -75,18 +75,17 @@ __global__ void __launch_bounds__(kTileBlock)
     if (i == n) tooffsets[n] = prefix + total;  // only the tile holding list n-1 ... n
   }
   if (l0 + kTileLists == n && threadIdx.x == 0) tooffsets[n] = prefix + total;
-  for (long long q = threadIdx.x; q < total; q += kTileBlock) {
-    const int r = tile_find(sm, q);
+  tile_for_each_slot(sm, total, [&](long long q, int r) {
     const long long j = s_slice[r] + (q - sm.loc[r]);
     long long idx = sliceindex[j];
     const long long count = s_count[r];
     if (idx < -count || idx >= count) {
       raise_error(err, inv, 4);
-      continue;
+      return;
     }
     if (idx < 0) idx += count;
     tocarry[prefix + q] = s_start[r] + idx;
-  }
+  });
 }
 
 // ------------------------------------------------------------------ carrylen

@@ -92,18 +92,33 @@ __global__ void __launch_bounds__(kTileBlock)
   }
 }
 
+// Four elements per thread and step, loads before stores (4 gathers in flight).
 template <class W>
 __global__ void take_kernel(W* __restrict__ out, const W* __restrict__ content,
                             const int64_t* __restrict__ carry, long long n, long long contentlen,
                             uint64_t inv, uint64_t* err) {
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    const long long c = __ldg(carry + i);
-    if (c < 0 || c >= contentlen) {
-      raise_error(err, inv, 0);
-      continue;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n; i0 += 4 * stride) {
+    long long c[4];
+    W v[4];
+    bool ok[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const long long i = i0 + k * stride;
+      c[k] = i < n ? __ldg(carry + i) : 0;
     }
-    out[i] = __ldg(content + c);
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      ok[k] = c[k] >= 0 && c[k] < contentlen;
+      v[k] = ok[k] ? __ldg(content + c[k]) : W(0);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const long long i = i0 + k * stride;
+      if (i >= n) continue;
+      if (ok[k]) out[i] = v[k];
+      else raise_error(err, inv, 0);
+    }
   }
 }
 

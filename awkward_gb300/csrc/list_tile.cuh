@@ -7,10 +7,10 @@
 // ticket counter, so every predecessor tile is already running): it scans
 // its lengths in shared memory, obtains the tile's global prefix with a
 // decoupled look-back (single pass, bounded spins), writes its offsets, and
-// then fills its outputs in output order -- consecutive threads write
-// consecutive slots, each slot finding its list by binary search over the
-// tile's local offsets.  The fill is therefore coalesced and balanced inside
-// the tile regardless of list lengths.
+// then fills its outputs in output order -- each warp a contiguous share of
+// the tile's slots, consecutive lanes on consecutive slots, each slot finding
+// its list by a forward walk over the tile's local offsets.  The fill is
+// therefore coalesced and balanced inside the tile regardless of list lengths.
 #pragma once
 
 #include "gb_common.cuh"
@@ -76,6 +76,34 @@ __device__ __forceinline__ int tile_find(const TileSmem& sm, long long q) {
     else hi = mid;
   }
   return lo;
+}
+
+// Visit every output slot q (0 <= q < total) of the tile with its list r.
+// With at least 4 slots per list on average each warp takes a contiguous
+// share, 32 consecutive slots per step (coalesced stores), and a lane finds
+// its list by walking forward from the list of the step's first slot; with
+// fewer a 32-slot step spans many lists, and a binary search per slot is
+// shorter than the walk.
+template <class F>
+__device__ __forceinline__ void tile_for_each_slot(const TileSmem& sm, long long total, F fn) {
+  if (total < 4ll * kTileLists) {
+    for (long long q = threadIdx.x; q < total; q += kTileBlock) fn(q, tile_find(sm, q));
+    return;
+  }
+  constexpr int kWarps = kTileBlock / 32;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long qa = total * warp / kWarps, qb = total * (warp + 1) / kWarps;
+  if (qa >= qb) return;
+  int r = tile_find(sm, qa);
+  for (long long g = qa; g < qb; g += 32) {
+    while (sm.loc[r + 1] <= g) r++;
+    const long long q = g + lane;
+    if (q < qb) {
+      int rl = r;
+      while (sm.loc[rl + 1] <= q) rl++;
+      fn(q, rl);
+    }
+  }
 }
 
 inline long long tile_count(long long n) { return (n + kTileLists - 1) / kTileLists; }

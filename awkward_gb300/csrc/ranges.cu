@@ -93,10 +93,9 @@ __global__ void __launch_bounds__(kTileBlock)
     if (i < n) tooffsets[i + 1] = (C)(prefix + sm.loc[li + 1]);
   }
   if (tile == 0 && threadIdx.x == 0) tooffsets[0] = 0;
-  for (long long q = threadIdx.x; q < total; q += kTileBlock) {
-    const int r = tile_find(sm, q);
+  tile_for_each_slot(sm, total, [&](long long q, int r) {
     tocarry[prefix + q] = s_first[r] + (q - sm.loc[r]) * step;
-  }
+  });
 }
 
 template <class C>
