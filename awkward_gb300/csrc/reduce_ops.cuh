@@ -412,6 +412,17 @@ struct ArgExtremumOp<double, MAX> {
   __device__ Out finalize(Acc a, long long) const { return a.idx; }
 };
 
+// Put the later cache sectors of a short run in flight before its loop walks
+// them (loads whose results are never read: nothing waits for them, so the
+// misses overlap instead of following one another).
+__device__ __forceinline__ void touch_run(const void* p, int n, int esize) {
+  const char* c = reinterpret_cast<const char*>(p);
+  long long d;
+  if (n > 4) asm volatile("ld.global.nc.b64 %0, [%1];" : "=l"(d) : "l"(c + 4 * esize));
+  if (n > 8) asm volatile("ld.global.nc.b64 %0, [%1];" : "=l"(d) : "l"(c + 8 * esize));
+  if (n > 12) asm volatile("ld.global.nc.b64 %0, [%1];" : "=l"(d) : "l"(c + 12 * esize));
+}
+
 // ---------------------------------------------------------------- short runs
 // Reduce n consecutive elements p[0..n) (global indices j0..j0+n) of one
 // list into a fresh accumulator.  The default steps element by element.
@@ -442,6 +453,7 @@ template <bool MAX>
 __device__ __forceinline__ typename ExtremumOp<double, MAX>::Acc run_short(
     const ExtremumOp<double, MAX>& op, const double* p, int n, long long j0, long long st,
     long long li) {
+  touch_run(p, n, 8);
   const long long* q = reinterpret_cast<const long long*>(p);
   long long best = 0;
   int at = -1;
@@ -500,6 +512,7 @@ __device__ __forceinline__ FxAcc run_short(const FixedSumOp<IN>& op, const IN* p
     // fixed point on the integer pipes; the double partial joins the fixed
     // point once (fx_add_f64 also carries its inf/NaN).  The result stays
     // within n*eps*sum|x| of the exact sum.
+    touch_run(p, n, 8);
     const long long* q = reinterpret_cast<const long long*>(p);
     const int* qh = reinterpret_cast<const int*>(p) + 1;
     double dsum = 0.0;
