@@ -176,6 +176,10 @@ __device__ __forceinline__ void seg_reduce_range(const Op& op,
       skip = li == I1 && small;  // the range where it ends takes all of it
       if (e < s0) e = s0;
     }
+    if (li + 32 <= last_list) {  // the next round's offsets in flight (result never read)
+      long long dd;
+      asm volatile("ld.global.nc.b64 %0, [%1];" : "=l"(dd) : "l"(offsets + li + 32));
+    }
     typename Op::Acc acc = op.identity();
     if (act && !skip && e - s0 <= kShortList) acc = run_short(op, x + s0, (int)(e - s0), s0, st, li);
     const bool longer = act && !skip && e - s0 > kShortList;
