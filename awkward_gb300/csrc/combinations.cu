@@ -164,8 +164,9 @@ __global__ void __launch_bounds__(kTileBlock)
   // walking forward from the list of the step's first slot.
   constexpr int kWarps = kTileBlock / 32;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if (n == 2 && total < (1ll << 31)) {
-    // pairs of a tile with fewer than 2^31 of them: tile-local positions in 32 bits
+  if ((n == 2 || n == 3) && total < (1ll << 31)) {
+    // pairs or triples of a tile with fewer than 2^31 of them: tile-local
+    // positions in 32 bits
     __shared__ int loc32[kTileLists + 1];
     for (int i = threadIdx.x; i <= kTileLists; i += kTileBlock) loc32[i] = (int)sm.loc[i];
     __syncthreads();
@@ -174,6 +175,7 @@ __global__ void __launch_bounds__(kTileBlock)
     if (qa >= qb) return;
     int64_t* __restrict__ out0 = s_ptr[0];
     int64_t* __restrict__ out1 = s_ptr[1];
+    int64_t* __restrict__ out2 = n == 3 ? s_ptr[2] : nullptr;
     const int shift = replacement ? 1 : 0;
     int r = tile_find(sm, qa);
     for (int g = qa; g < qb; g += 32) {
@@ -185,6 +187,42 @@ __global__ void __launch_bounds__(kTileBlock)
       const int rank = q - loc32[rl];
       const long long s = s_size[rl];
       const long long base = s_start[rl];
+      if (n == 3) {
+        long long p0, p1, p2;
+        if (s < 1024) {  // C(s,3) < 2^31: every product in 32 bits
+          const int si = (int)s;
+          auto c3 = [](int m) { return m < 3 ? 0 : (m * (m - 1) * (m - 2)) / 6; };
+          const int tot = c3(si);
+          int lo = 0, hi = si - 3;
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (tot - c3(si - mid) <= rank) lo = mid;
+            else hi = mid - 1;
+          }
+          int a2, b2;
+          unrank2_small(si - lo - 1, rank - (tot - c3(si - lo)), &a2, &b2);
+          p0 = lo;
+          p1 = lo + 1 + a2;
+          p2 = lo + 1 + b2;
+        } else {
+          const long long tot = binom3(s);
+          long long lo = 0, hi = s - 3;
+          while (lo < hi) {
+            const long long mid = (lo + hi + 1) >> 1;
+            if (tot - binom3(s - mid) <= rank) lo = mid;
+            else hi = mid - 1;
+          }
+          long long a2, b2;
+          unrank2(s - lo - 1, rank - (tot - binom3(s - lo)), &a2, &b2);
+          p0 = lo;
+          p1 = lo + 1 + a2;
+          p2 = lo + 1 + b2;
+        }
+        out0[prefix + q] = base + p0;
+        out1[prefix + q] = base + p1 - shift;
+        out2[prefix + q] = base + p2 - 2 * shift;
+        continue;
+      }
       long long a, b;
       if (s < (1ll << 15)) {
         int ai, bi;
