@@ -29,6 +29,12 @@ _FAMILY_MESSAGES = {
         "stops[i] < starts[i]",
         "cannot fit jagged slice into nested list",
     ],
+    # awkward_ListArray_broadcast_tooffsets.cu:18-22
+    "awkward_ListArray_broadcast_tooffsets": [
+        "stops[i] > len(content)",
+        "broadcast's offsets must be monotonically increasing",
+        "cannot broadcast nested list",
+    ],
     # awkward_ListArray_getitem_jagged_numvalid.cu:14-17
     "awkward_ListArray_getitem_jagged_numvalid": [
         "jagged slice's stops[i] < starts[i]",

@@ -298,7 +298,91 @@ __global__ void __launch_bounds__(kTileBlock)
   }
 }
 
+// RegularArray combinations: list i is [size*i, size*i + size), every list
+// has the same tuple count c, so slot q belongs to list q / c with rank q % c.
+__global__ void regular_combinations_kernel(int64_t** __restrict__ tocarry, long long n,
+                                            bool replacement, long long size, long long length,
+                                            long long per_list) {
+  __shared__ int64_t* s_ptr[kMaxPtrs];
+  if (threadIdx.x < kMaxPtrs && threadIdx.x < n) s_ptr[threadIdx.x] = tocarry[threadIdx.x];
+  __syncthreads();
+  const long long s = replacement ? size + n - 1 : size;
+  const long long total = per_list * length;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
+       q += (long long)gridDim.x * blockDim.x) {
+    const long long i = q / per_list;
+    long long rank = q - i * per_list;
+    const long long base = size * i;
+    if (n == 1) {
+      s_ptr[0][q] = base + rank;
+    } else if (n == 2) {
+      long long a, b;
+      unrank2(s, rank, &a, &b);
+      s_ptr[0][q] = base + a;
+      s_ptr[1][q] = base + (replacement ? b - 1 : b);
+    } else {
+      long long lo = 0;
+      for (long long p = 0; p < n; p++) {
+        const long long rem = n - p;
+        const long long here = binom(s - lo, rem);
+        long long vlo = lo, vhi = s - rem;
+        while (vlo < vhi) {
+          const long long mid = (vlo + vhi + 1) >> 1;
+          if (here - binom(s - mid, rem) <= rank) vlo = mid;
+          else vhi = mid - 1;
+        }
+        rank -= here - binom(s - vlo, rem);
+        int64_t* dst = p < kMaxPtrs ? s_ptr[p] : tocarry[p];
+        dst[q] = base + (replacement ? vlo - p : vlo);
+        lo = vlo + 1;
+      }
+    }
+  }
+}
+
+__global__ void fill_kernel(int64_t* __restrict__ dst, long long n, long long value) {
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) dst[i] = value;
+}
+
+long long combinations_count_host(long long size, long long n, bool replacement) {
+  if (replacement) size += n - 1;
+  long long thisn = n;
+  if (thisn > size) return 0;
+  if (thisn == size) return 1;
+  if (thisn * 2 > size) thisn = size - thisn;
+  long long len = size;
+  for (long long j = 2; j <= thisn; j++) {
+    len *= (size - j + 1);
+    len /= j;
+  }
+  return len;
+}
+
 }  // namespace
+
+// awkward_RegularArray_combinations_64.cpp:8-29.  toindex[k] receives the
+// total (the CPU's final counters); fromindex is the CPU's scratch cursor.
+GB_EXPORT int awkward_RegularArray_combinations_64(int64_t** tocarry, int64_t* toindex,
+                                                   int64_t* fromindex, int64_t n, bool replacement,
+                                                   int64_t size, int64_t length,
+                                                   uint64_t invocation_index, uint64_t* err_code,
+                                                   void* stream) {
+  (void)fromindex;
+  (void)invocation_index;
+  (void)err_code;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (n <= 0) return 0;
+  const long long per_list = length > 0 ? combinations_count_host(size, n, replacement) : 0;
+  const long long total = per_list * (length > 0 ? length : 0);
+  fill_kernel<<<1, 32, 0, s>>>(toindex, n, total);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || total <= 0) return (int)e;
+  long long g = (total + 255) / 256;
+  const long long cap = (long long)device_sm_count() * 32;
+  regular_combinations_kernel<<<(unsigned)(g < cap ? g : cap), 256, 0, s>>>(
+      tocarry, n, replacement, size, length, per_list);
+  return (int)cudaGetLastError();
+}
 
 #define GB_COMB_LENGTH(NAME, C)                                                                 \
   GB_EXPORT int NAME(int64_t* totallen, int64_t* tooffsets, int64_t n, bool replacement,       \

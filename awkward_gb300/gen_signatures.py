@@ -63,6 +63,9 @@ FAMILIES = {
     # combinations
     "awkward_ListArray_combinations_length": ("awkward_ListArray_combinations_length.cpp", 8),
     "awkward_ListArray_combinations": ("awkward_ListArray_combinations.cpp", 9),
+    # siblings of combinations and jagged broadcasting
+    "awkward_RegularArray_combinations_64": ("awkward_RegularArray_combinations_64.cpp", 8),
+    "awkward_ListArray_broadcast_tooffsets": ("awkward_ListArray_broadcast_tooffsets.cpp", 8),
 }
 
 _C_TYPES = {

@@ -38,6 +38,13 @@ extern "C" {
 #define AWKWARD_GB300_ERROR_BITS 8
 #define AWKWARD_GB300_NO_ERROR 0xffffffffffffffffULL
 
+/* ---- awkward_ListArray_broadcast_tooffsets: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_broadcast_tooffsets.cpp:8 */
+/* kernel-specification.yml:1080 */
+int awkward_ListArray32_broadcast_tooffsets_64(int64_t* tocarry, const int64_t* fromoffsets, int64_t offsetslength, const int32_t* fromstarts, const int32_t* fromstops, int64_t lencontent, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1088 */
+int awkward_ListArray64_broadcast_tooffsets_64(int64_t* tocarry, const int64_t* fromoffsets, int64_t offsetslength, const int64_t* fromstarts, const int64_t* fromstops, int64_t lencontent, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1096 */
+int awkward_ListArrayU32_broadcast_tooffsets_64(int64_t* tocarry, const int64_t* fromoffsets, int64_t offsetslength, const uint32_t* fromstarts, const uint32_t* fromstops, int64_t lencontent, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_ListArray_combinations: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_combinations.cpp:9 */
 /* kernel-specification.yml:1127 */
 int awkward_ListArray32_combinations_64(int64_t** tocarry, int64_t* toindex, int64_t* fromindex, int64_t n, bool replacement, const int32_t* starts, const int32_t* stops, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
@@ -109,6 +116,9 @@ int awkward_NumpyArray_reduce_adjust_starts_64(int64_t* toptr, int64_t outlength
 /* ---- awkward_NumpyArray_reduce_mask_ByteMaskedArray_64: replaces awkward-cpp/src/cpu-kernels/awkward_NumpyArray_reduce_mask_ByteMaskedArray_64.cpp:7 */
 /* kernel-specification.yml:2587 */
 int awkward_NumpyArray_reduce_mask_ByteMaskedArray_64(int8_t* toptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_RegularArray_combinations_64: replaces awkward-cpp/src/cpu-kernels/awkward_RegularArray_combinations_64.cpp:8 */
+/* kernel-specification.yml:2868 */
+int awkward_RegularArray_combinations_64(int64_t** tocarry, int64_t* toindex, int64_t* fromindex, int64_t n, bool replacement, int64_t size, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_RegularArray_getitem_jagged_expand: replaces awkward-cpp/src/cpu-kernels/awkward_RegularArray_getitem_jagged_expand.cpp:8 */
 /* kernel-specification.yml:2912 */
 int awkward_RegularArray_getitem_jagged_expand_64(int64_t* multistarts, int64_t* multistops, const int64_t* singleoffsets, int64_t regularsize, int64_t regularlength, uint64_t invocation_index, uint64_t* err_code, void* stream);

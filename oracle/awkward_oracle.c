@@ -636,6 +636,46 @@ ORACLE_COMBINATIONS(awkward_ListArray32_combinations_64, int32_t)
 ORACLE_COMBINATIONS(awkward_ListArrayU32_combinations_64, uint32_t)
 ORACLE_COMBINATIONS(awkward_ListArray64_combinations_64, int64_t)
 
+/* awkward_RegularArray_combinations_64.cpp:8-29: every list is [size*i, size*i + size) */
+struct Error awkward_RegularArray_combinations_64(int64_t** tocarry, int64_t* toindex,
+                                                  int64_t* fromindex, int64_t n, bool replacement,
+                                                  int64_t size, int64_t length) {
+  for (int64_t j = 0; j < n; j++) toindex[j] = 0;
+  for (int64_t i = 0; i < length; i++) {
+    int64_t start = size * i;
+    fromindex[0] = start;
+    oracle_combinations_step(tocarry, toindex, fromindex, 0, start + size, n, replacement);
+  }
+  return success();
+}
+
+/* ======================================================================
+ * Broadcast of a ListArray to given offsets
+ * (awkward_ListArray_broadcast_tooffsets.cpp:8-33)
+ * ====================================================================== */
+#define ORACLE_BROADCAST_TOOFFSETS(NAME, C)                                    \
+  struct Error NAME(int64_t* tocarry, const int64_t* fromoffsets,              \
+                    int64_t offsetslength, const C* fromstarts,                \
+                    const C* fromstops, int64_t lencontent) {                  \
+    int64_t k = 0;                                                             \
+    for (int64_t i = 0; i < offsetslength - 1; i++) {                          \
+      int64_t start = (int64_t)fromstarts[i], stop = (int64_t)fromstops[i];    \
+      if (start != stop && stop > lencontent)                                  \
+        return failure("stops[i] > len(content)", i, stop);                    \
+      int64_t count = fromoffsets[i + 1] - fromoffsets[i];                     \
+      if (count < 0)                                                           \
+        return failure("broadcast's offsets must be monotonically increasing", \
+                       i, kSliceNone);                                         \
+      if (stop - start != count)                                               \
+        return failure("cannot broadcast nested list", i, kSliceNone);         \
+      for (int64_t j = start; j < stop; j++) tocarry[k++] = j;                 \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_BROADCAST_TOOFFSETS(awkward_ListArray32_broadcast_tooffsets_64, int32_t)
+ORACLE_BROADCAST_TOOFFSETS(awkward_ListArrayU32_broadcast_tooffsets_64, uint32_t)
+ORACLE_BROADCAST_TOOFFSETS(awkward_ListArray64_broadcast_tooffsets_64, int64_t)
+
 /* ======================================================================
  * Multi-core driver for the CPU baseline: run one reducer (any of the
  * (toptr, fromptr, offsets, outlength) family above, or argmax/argmin with

@@ -86,7 +86,11 @@ def build_ref(awkward_src=None, force=False):
 
     files = sorted({rec["cpu"].split(":")[0].split("/")[-1] for rec in SIGNATURES.values()})
     sources = [os.path.join(kdir, f) for f in files] + [os.path.join(kdir, "kernel-utils.cpp")]
-    if not (force or _stale(REF_SO, sources)):
+    # the set of compiled files changes when families are added: rebuild then too
+    manifest = REF_SO + ".sources"
+    listed = open(manifest).read() if os.path.exists(manifest) else ""
+    wanted = "\n".join(sources)
+    if not (force or _stale(REF_SO, sources) or listed != wanted):
         return REF_SO
     hdr = os.path.join(REF_DIR, "include", "awkward", "kernels.h")
     _write_ref_header(hdr)
@@ -94,6 +98,8 @@ def build_ref(awkward_src=None, force=False):
            "-I", os.path.join(REF_DIR, "include"), "-I", inc, *sources, "-o", REF_SO + ".tmp"]
     subprocess.check_call(cmd)
     os.replace(REF_SO + ".tmp", REF_SO)
+    with open(manifest, "w") as f:
+        f.write(wanted)
     return REF_SO
 
 

@@ -22,6 +22,7 @@ from __future__ import annotations
 import json
 import os
 import sys
+import zlib
 
 import numpy as np
 
@@ -241,8 +242,47 @@ def combinations_cases(rng, name):
     return out
 
 
+def regular_combinations_cases(rng, name):
+    out = []
+    for n_, repl, size in [(2, False, 5), (3, False, 6), (2, True, 4), (3, True, 3), (1, False, 4),
+                           (4, False, 7), (2, False, 1), (3, False, 0)]:
+        length = 40
+        tmp_total = np.zeros(1, np.int64)
+        starts = (np.arange(length) * size).astype(np.int64)
+        oracle.call(oracle.load_ref(), "awkward_ListArray64_combinations_length_64",
+                    totallen=tmp_total, tooffsets=np.zeros(length + 1, np.int64), n=n_,
+                    replacement=repl, starts=starts, stops=starts + size, length=length)
+        total = int(tmp_total[0])
+        out.append({"tocarry": [np.full(total, 123, np.int64) for _ in range(n_)],
+                    "toindex": np.full(n_, 123, np.int64), "fromindex": np.zeros(n_, np.int64),
+                    "n": n_, "replacement": repl, "size": size, "length": length})
+    return out
+
+
+def broadcast_cases(rng, name):
+    C = NP_DTYPES[{a[0]: a for a in SIGNATURES[name]["args"]}["fromstarts"][1]]
+    out = []
+    for variant in ("valid", "gaps", "mismatch"):
+        n = 200
+        L = _lengths(rng, n, 5, longs=(40,))
+        off = _offsets(L) + 3
+        if variant == "gaps":  # a ListArray whose lists are not contiguous
+            starts = np.cumsum(L + rng.integers(0, 3, n)) - L
+        else:
+            starts = off[:-1] - 3
+        stops = starts + L
+        if variant == "mismatch":
+            stops = stops.copy()
+            stops[rng.integers(0, n)] += 1
+        lencontent = int(stops.max()) + 2 if n else 0
+        out.append({"tocarry": np.full(int(off[-1] - off[0]) + 4, 123, np.int64), "fromoffsets": off,
+                    "offsetslength": n + 1, "fromstarts": starts.astype(C),
+                    "fromstops": stops.astype(C), "lencontent": lencontent})
+    return out
+
+
 def make_random():
-    rng = np.random.default_rng(20241203)
+    ref = oracle.load_ref()
     ref = oracle.load_ref()
     if ref is None:
         raise SystemExit("awkward-cpp CPU kernels not built (oracle/build.py)")
@@ -250,7 +290,13 @@ def make_random():
     arrays = {}
     for name, rec in SIGNATURES.items():
         fam = rec["family"]
-        if fam.startswith(("awkward_reduce", "awkward_NumpyArray_reduce")):
+        # one generator per specialization: adding a family leaves the others' cases unchanged
+        rng = np.random.default_rng([20241203, zlib.crc32(name.encode())])
+        if fam == "awkward_RegularArray_combinations_64":
+            cases = regular_combinations_cases(rng, name)
+        elif fam == "awkward_ListArray_broadcast_tooffsets":
+            cases = broadcast_cases(rng, name)
+        elif fam.startswith(("awkward_reduce", "awkward_NumpyArray_reduce")):
             cases = [reducer_case(rng, name)]
         elif "next_range" in fam:
             cases = range_cases(rng, name)
