@@ -66,6 +66,9 @@ FAMILIES = {
     # siblings of combinations and jagged broadcasting
     "awkward_RegularArray_combinations_64": ("awkward_RegularArray_combinations_64.cpp", 8),
     "awkward_ListArray_broadcast_tooffsets": ("awkward_ListArray_broadcast_tooffsets.cpp", 8),
+    # segmented sort
+    "awkward_argsort": ("awkward_argsort.cpp", 62),
+    "awkward_sort": ("awkward_sort.cpp", 62),
 }
 
 _C_TYPES = {

@@ -125,6 +125,95 @@ int awkward_RegularArray_getitem_jagged_expand_64(int64_t* multistarts, int64_t*
 /* ---- awkward_RegularArray_getitem_next_range: replaces awkward-cpp/src/cpu-kernels/awkward_RegularArray_getitem_next_range.cpp:8 */
 /* kernel-specification.yml:3014 */
 int awkward_RegularArray_getitem_next_range_64(int64_t* tocarry, int64_t regular_start, int64_t step, int64_t length, int64_t size, int64_t nextsize, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_argsort: replaces awkward-cpp/src/cpu-kernels/awkward_argsort.cpp:62 */
+/* kernel-specification.yml:3724 */
+int awkward_argsort_bool_int32(int64_t* toptr, const bool* fromptr, int64_t length, const int32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3733 */
+int awkward_argsort_bool_uint32(int64_t* toptr, const bool* fromptr, int64_t length, const uint32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3742 */
+int awkward_argsort_bool_uint64(int64_t* toptr, const bool* fromptr, int64_t length, const uint64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3751 */
+int awkward_argsort_bool_int64(int64_t* toptr, const bool* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3760 */
+int awkward_argsort_int8_int32(int64_t* toptr, const int8_t* fromptr, int64_t length, const int32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3769 */
+int awkward_argsort_int8_uint32(int64_t* toptr, const int8_t* fromptr, int64_t length, const uint32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3778 */
+int awkward_argsort_int8_uint64(int64_t* toptr, const int8_t* fromptr, int64_t length, const uint64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3787 */
+int awkward_argsort_int8_int64(int64_t* toptr, const int8_t* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3796 */
+int awkward_argsort_int16_int32(int64_t* toptr, const int16_t* fromptr, int64_t length, const int32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3805 */
+int awkward_argsort_int16_uint32(int64_t* toptr, const int16_t* fromptr, int64_t length, const uint32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3814 */
+int awkward_argsort_int16_uint64(int64_t* toptr, const int16_t* fromptr, int64_t length, const uint64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3823 */
+int awkward_argsort_int16_int64(int64_t* toptr, const int16_t* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3832 */
+int awkward_argsort_int32_int32(int64_t* toptr, const int32_t* fromptr, int64_t length, const int32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3841 */
+int awkward_argsort_int32_uint32(int64_t* toptr, const int32_t* fromptr, int64_t length, const uint32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3850 */
+int awkward_argsort_int32_uint64(int64_t* toptr, const int32_t* fromptr, int64_t length, const uint64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3859 */
+int awkward_argsort_int32_int64(int64_t* toptr, const int32_t* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3868 */
+int awkward_argsort_int64_int32(int64_t* toptr, const int64_t* fromptr, int64_t length, const int32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3877 */
+int awkward_argsort_int64_uint32(int64_t* toptr, const int64_t* fromptr, int64_t length, const uint32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3886 */
+int awkward_argsort_int64_uint64(int64_t* toptr, const int64_t* fromptr, int64_t length, const uint64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3895 */
+int awkward_argsort_int64_int64(int64_t* toptr, const int64_t* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3904 */
+int awkward_argsort_uint8_int32(int64_t* toptr, const uint8_t* fromptr, int64_t length, const int32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3913 */
+int awkward_argsort_uint8_uint32(int64_t* toptr, const uint8_t* fromptr, int64_t length, const uint32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3922 */
+int awkward_argsort_uint8_uint64(int64_t* toptr, const uint8_t* fromptr, int64_t length, const uint64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3931 */
+int awkward_argsort_uint8_int64(int64_t* toptr, const uint8_t* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3940 */
+int awkward_argsort_uint16_int32(int64_t* toptr, const uint16_t* fromptr, int64_t length, const int32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3949 */
+int awkward_argsort_uint16_uint32(int64_t* toptr, const uint16_t* fromptr, int64_t length, const uint32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3958 */
+int awkward_argsort_uint16_uint64(int64_t* toptr, const uint16_t* fromptr, int64_t length, const uint64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3967 */
+int awkward_argsort_uint16_int64(int64_t* toptr, const uint16_t* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3976 */
+int awkward_argsort_uint32_int32(int64_t* toptr, const uint32_t* fromptr, int64_t length, const int32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3985 */
+int awkward_argsort_uint32_uint32(int64_t* toptr, const uint32_t* fromptr, int64_t length, const uint32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:3994 */
+int awkward_argsort_uint32_uint64(int64_t* toptr, const uint32_t* fromptr, int64_t length, const uint64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4003 */
+int awkward_argsort_uint32_int64(int64_t* toptr, const uint32_t* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4012 */
+int awkward_argsort_uint64_int32(int64_t* toptr, const uint64_t* fromptr, int64_t length, const int32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4021 */
+int awkward_argsort_uint64_uint32(int64_t* toptr, const uint64_t* fromptr, int64_t length, const uint32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4030 */
+int awkward_argsort_uint64_uint64(int64_t* toptr, const uint64_t* fromptr, int64_t length, const uint64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4039 */
+int awkward_argsort_uint64_int64(int64_t* toptr, const uint64_t* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4048 */
+int awkward_argsort_float32_int32(int64_t* toptr, const float* fromptr, int64_t length, const int32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4057 */
+int awkward_argsort_float32_uint32(int64_t* toptr, const float* fromptr, int64_t length, const uint32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4066 */
+int awkward_argsort_float32_uint64(int64_t* toptr, const float* fromptr, int64_t length, const uint64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4075 */
+int awkward_argsort_float32_int64(int64_t* toptr, const float* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4084 */
+int awkward_argsort_float64_int32(int64_t* toptr, const double* fromptr, int64_t length, const int32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4093 */
+int awkward_argsort_float64_uint32(int64_t* toptr, const double* fromptr, int64_t length, const uint32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4102 */
+int awkward_argsort_float64_uint64(int64_t* toptr, const double* fromptr, int64_t length, const uint64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4111 */
+int awkward_argsort_float64_int64(int64_t* toptr, const double* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_reduce_argmax: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_argmax.cpp:9 */
 /* kernel-specification.yml:4227 */
 int awkward_reduce_argmax_int8_64(int64_t* toptr, const int8_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
@@ -440,6 +529,29 @@ int awkward_reduce_sum_int32_bool_64(int32_t* toptr, const bool* fromptr, const 
 /* ---- awkward_reduce_sum_int64_bool_64: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_sum_int64_bool_64.cpp:7 */
 /* kernel-specification.yml:5601 */
 int awkward_reduce_sum_int64_bool_64(int64_t* toptr, const bool* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_sort: replaces awkward-cpp/src/cpu-kernels/awkward_sort.cpp:62 */
+/* kernel-specification.yml:5619 */
+int awkward_sort_bool(bool* toptr, const bool* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5628 */
+int awkward_sort_int8(int8_t* toptr, const int8_t* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5637 */
+int awkward_sort_int16(int16_t* toptr, const int16_t* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5646 */
+int awkward_sort_int32(int32_t* toptr, const int32_t* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5655 */
+int awkward_sort_int64(int64_t* toptr, const int64_t* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5664 */
+int awkward_sort_uint8(uint8_t* toptr, const uint8_t* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5673 */
+int awkward_sort_uint16(uint16_t* toptr, const uint16_t* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5682 */
+int awkward_sort_uint32(uint32_t* toptr, const uint32_t* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5691 */
+int awkward_sort_uint64(uint64_t* toptr, const uint64_t* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5700 */
+int awkward_sort_float32(float* toptr, const float* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5709 */
+int awkward_sort_float64(double* toptr, const double* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
 
 /* ---- no-alloc variant.  No counterpart in awkward: an extra entry point
  * of this library for callers that may not allocate device memory while

@@ -28,6 +28,7 @@
 #include <stddef.h>
 #include <stdint.h>
 #include <stdlib.h>
+#include <string.h>
 
 struct Error {
   const char* str;
@@ -675,6 +676,128 @@ struct Error awkward_RegularArray_combinations_64(int64_t** tocarry, int64_t* to
 ORACLE_BROADCAST_TOOFFSETS(awkward_ListArray32_broadcast_tooffsets_64, int32_t)
 ORACLE_BROADCAST_TOOFFSETS(awkward_ListArrayU32_broadcast_tooffsets_64, uint32_t)
 ORACLE_BROADCAST_TOOFFSETS(awkward_ListArray64_broadcast_tooffsets_64, int64_t)
+
+/* ======================================================================
+ * Segmented sort (awkward_argsort.cpp:62-108, awkward_sort.cpp:62-117)
+ * ====================================================================== */
+
+/* The comparators of awkward_argsort.cpp:23-59 / awkward_sort.cpp:23-59:
+ * integers and bool compare directly; floating point puts NaN before every
+ * number in both directions. */
+typedef int (*oracle_less_fn)(const void* x, int64_t a, int64_t b, int asc);
+#define ORACLE_LESS_INT(NAME, T)                                               \
+  static int NAME(const void* x, int64_t a, int64_t b, int asc) {              \
+    T l = ((const T*)x)[a], r = ((const T*)x)[b];                              \
+    return asc ? (l < r) : (l > r);                                            \
+  }
+#define ORACLE_LESS_FLT(NAME, T)                                               \
+  static int NAME(const void* x, int64_t a, int64_t b, int asc) {              \
+    T l = ((const T*)x)[a], r = ((const T*)x)[b];                              \
+    return !isnan(r) && (isnan(l) || (asc ? l < r : l > r));                   \
+  }
+ORACLE_LESS_INT(oracle_less_bool, bool)
+ORACLE_LESS_INT(oracle_less_int8, int8_t)
+ORACLE_LESS_INT(oracle_less_uint8, uint8_t)
+ORACLE_LESS_INT(oracle_less_int16, int16_t)
+ORACLE_LESS_INT(oracle_less_uint16, uint16_t)
+ORACLE_LESS_INT(oracle_less_int32, int32_t)
+ORACLE_LESS_INT(oracle_less_uint32, uint32_t)
+ORACLE_LESS_INT(oracle_less_int64, int64_t)
+ORACLE_LESS_INT(oracle_less_uint64, uint64_t)
+ORACLE_LESS_FLT(oracle_less_float32, float)
+ORACLE_LESS_FLT(oracle_less_float64, double)
+
+/* Stable sort of idx[0..n) by x[idx[.]] (std::stable_sort's contract):
+ * bottom-up merge, taking from the right run only when strictly less. */
+static void oracle_stable_sort(int64_t* idx, int64_t n, const void* x, oracle_less_fn less,
+                               int asc) {
+  if (n < 2) return;
+  int64_t* tmp = (int64_t*)malloc((size_t)n * sizeof(int64_t));
+  int64_t* a = idx;
+  int64_t* b = tmp;
+  for (int64_t w = 1; w < n; w *= 2) {
+    for (int64_t lo = 0; lo < n; lo += 2 * w) {
+      int64_t mid = lo + w < n ? lo + w : n, hi = lo + 2 * w < n ? lo + 2 * w : n;
+      int64_t i = lo, j = mid, k = lo;
+      while (i < mid && j < hi) b[k++] = less(x, a[j], a[i], asc) ? a[j++] : a[i++];
+      while (i < mid) b[k++] = a[i++];
+      while (j < hi) b[k++] = a[j++];
+    }
+    int64_t* t = a;
+    a = b;
+    b = t;
+  }
+  if (a != idx) memcpy(idx, a, (size_t)n * sizeof(int64_t));
+  free(tmp);
+}
+
+/* argsort: iota, each clamped segment sorted (stable), then made local. */
+#define ORACLE_ARGSORT(NAME, T, U, LESS)                                       \
+  struct Error NAME(int64_t* toptr, const T* fromptr, int64_t length,          \
+                    const U* offsets, int64_t offsetslength, bool ascending,   \
+                    bool stable) {                                             \
+    (void)stable;                                                              \
+    for (int64_t i = 0; i < length; i++) toptr[i] = i;                         \
+    for (int64_t i = 0; i < offsetslength - 1; i++) {                          \
+      int64_t st = (int64_t)offsets[i], sp = (int64_t)offsets[i + 1];          \
+      if (st > length) st = length;                                            \
+      if (sp > length) sp = length;                                            \
+      if (st >= sp) continue;                                                  \
+      oracle_stable_sort(toptr + st, sp - st, fromptr, LESS, ascending);      \
+      for (int64_t j = st; j < sp; j++) toptr[j] -= st;                        \
+    }                                                                          \
+    return success();                                                          \
+  }
+#define ORACLE_ARGSORT_ALL(T, SUF, LESS)                                       \
+  ORACLE_ARGSORT(awkward_argsort_##SUF##_int32, T, int32_t, LESS)              \
+  ORACLE_ARGSORT(awkward_argsort_##SUF##_uint32, T, uint32_t, LESS)            \
+  ORACLE_ARGSORT(awkward_argsort_##SUF##_uint64, T, uint64_t, LESS)            \
+  ORACLE_ARGSORT(awkward_argsort_##SUF##_int64, T, int64_t, LESS)
+ORACLE_ARGSORT_ALL(bool, bool, oracle_less_bool)
+ORACLE_ARGSORT_ALL(int8_t, int8, oracle_less_int8)
+ORACLE_ARGSORT_ALL(uint8_t, uint8, oracle_less_uint8)
+ORACLE_ARGSORT_ALL(int16_t, int16, oracle_less_int16)
+ORACLE_ARGSORT_ALL(uint16_t, uint16, oracle_less_uint16)
+ORACLE_ARGSORT_ALL(int32_t, int32, oracle_less_int32)
+ORACLE_ARGSORT_ALL(uint32_t, uint32, oracle_less_uint32)
+ORACLE_ARGSORT_ALL(int64_t, int64, oracle_less_int64)
+ORACLE_ARGSORT_ALL(uint64_t, uint64, oracle_less_uint64)
+ORACLE_ARGSORT_ALL(float, float32, oracle_less_float32)
+ORACLE_ARGSORT_ALL(double, float64, oracle_less_float64)
+
+/* sort: the same on an index, then the first min(offsets[last], length)
+ * values gathered through it. */
+#define ORACLE_SORT(NAME, T, LESS)                                             \
+  struct Error NAME(T* toptr, const T* fromptr, int64_t length,                \
+                    const int64_t* offsets, int64_t offsetslength,             \
+                    bool ascending, bool stable) {                             \
+    (void)stable;                                                              \
+    int64_t* index = (int64_t*)malloc((size_t)(length > 0 ? length : 1) * sizeof(int64_t)); \
+    for (int64_t i = 0; i < length; i++) index[i] = i;                         \
+    for (int64_t i = 0; i < offsetslength - 1; i++) {                          \
+      int64_t st = offsets[i], sp = offsets[i + 1];                            \
+      if (st > length) st = length;                                            \
+      if (sp > length) sp = length;                                            \
+      if (st >= sp) continue;                                                  \
+      oracle_stable_sort(index + st, sp - st, fromptr, LESS, ascending);      \
+    }                                                                          \
+    int64_t total = offsetslength > 0 ? offsets[offsetslength - 1] : 0;        \
+    int64_t copy = total < length ? total : length;                            \
+    for (int64_t i = 0; i < copy; i++) toptr[i] = fromptr[index[i]];           \
+    free(index);                                                               \
+    return success();                                                          \
+  }
+ORACLE_SORT(awkward_sort_bool, bool, oracle_less_bool)
+ORACLE_SORT(awkward_sort_int8, int8_t, oracle_less_int8)
+ORACLE_SORT(awkward_sort_uint8, uint8_t, oracle_less_uint8)
+ORACLE_SORT(awkward_sort_int16, int16_t, oracle_less_int16)
+ORACLE_SORT(awkward_sort_uint16, uint16_t, oracle_less_uint16)
+ORACLE_SORT(awkward_sort_int32, int32_t, oracle_less_int32)
+ORACLE_SORT(awkward_sort_uint32, uint32_t, oracle_less_uint32)
+ORACLE_SORT(awkward_sort_int64, int64_t, oracle_less_int64)
+ORACLE_SORT(awkward_sort_uint64, uint64_t, oracle_less_uint64)
+ORACLE_SORT(awkward_sort_float32, float, oracle_less_float32)
+ORACLE_SORT(awkward_sort_float64, double, oracle_less_float64)
 
 /* ======================================================================
  * Multi-core driver for the CPU baseline: run one reducer (any of the

@@ -281,6 +281,44 @@ def broadcast_cases(rng, name):
     return out
 
 
+def sort_cases(rng, name):
+    rec = SIGNATURES[name]
+    args = {a[0]: a for a in rec["args"]}
+    base = args["fromptr"][1]
+    U = NP_DTYPES[args["offsets"][1]]
+    out = []
+    for ascending, stable in [(True, True), (False, True), (True, False), (False, False)]:
+        if not stable and base in ("bool", "int8_t", "uint8_t"):
+            continue  # too few distinct values for a tie-free unstable case
+        n = 120
+        # the merged path (segments past 2048 elements) in the 64-bit cases only
+        wide = base in ("double", "int64_t") and args["offsets"][1] == "int64_t"
+        L = _lengths(rng, n, 6, longs=(33, 257, 2050, 5000) if wide else (33, 257))
+        off = _offsets(L)
+        E = int(off[-1])
+        if stable:
+            x = _values(rng, base, E)
+        else:  # distinct values: std::sort's order is then unique
+            dt = NP_DTYPES[base]
+            if base in ("float", "double"):
+                x = (rng.permutation(E) - E / 2).astype(dt) / 7
+            else:
+                info = np.iinfo(dt)
+                span = min(int(info.max) - int(info.min), 1 << 40)
+                x = (rng.permutation(E) % span + (int(info.min) if int(info.min) < 0 else 0)).astype(dt)
+        length = E + 3
+        xx = np.concatenate([x, np.zeros(3, x.dtype)]) if E else np.zeros(3, NP_DTYPES[base])
+        if name.startswith("awkward_argsort"):
+            out.append({"toptr": np.full(length, 123, np.int64), "fromptr": xx, "length": length,
+                        "offsets": off.astype(U), "offsetslength": n + 1,
+                        "ascending": ascending, "stable": stable})
+        else:
+            out.append({"toptr": np.full(length, 123, NP_DTYPES[base]), "fromptr": xx,
+                        "length": length, "offsets": off, "offsetslength": n + 1,
+                        "ascending": ascending, "stable": stable})
+    return out
+
+
 def make_random():
     ref = oracle.load_ref()
     ref = oracle.load_ref()
@@ -292,7 +330,9 @@ def make_random():
         fam = rec["family"]
         # one generator per specialization: adding a family leaves the others' cases unchanged
         rng = np.random.default_rng([20241203, zlib.crc32(name.encode())])
-        if fam == "awkward_RegularArray_combinations_64":
+        if fam in ("awkward_argsort", "awkward_sort"):
+            cases = sort_cases(rng, name)
+        elif fam == "awkward_RegularArray_combinations_64":
             cases = regular_combinations_cases(rng, name)
         elif fam == "awkward_ListArray_broadcast_tooffsets":
             cases = broadcast_cases(rng, name)
