@@ -69,6 +69,23 @@ FAMILIES = {
     # segmented sort
     "awkward_argsort": ("awkward_argsort.cpp", 62),
     "awkward_sort": ("awkward_sort.cpp", 62),
+    # reductions above the innermost axis (non-local) and through option types
+    "awkward_ListOffsetArray_reduce_nonlocal_maxcount_offsetscopy_64": ("awkward_ListOffsetArray_reduce_nonlocal_maxcount_offsetscopy_64.cpp", 7),
+    "awkward_ListOffsetArray_reduce_nonlocal_preparenext_64": ("awkward_ListOffsetArray_reduce_nonlocal_preparenext_64.cpp", 7),
+    "awkward_ListOffsetArray_reduce_nonlocal_outstartsstops_64": ("awkward_ListOffsetArray_reduce_nonlocal_outstartsstops_64.cpp", 10),
+    "awkward_ListOffsetArray_reduce_nonlocal_nextshifts_64": ("awkward_ListOffsetArray_reduce_nonlocal_nextshifts_64.cpp", 7),
+    "awkward_ListOffsetArray_reduce_local_nextparents_64": ("awkward_ListOffsetArray_reduce_local_nextparents_64.cpp", 14),
+    "awkward_ListOffsetArray_local_preparenext_64": ("awkward_ListOffsetArray_local_preparenext_64.cpp", 11),
+    "awkward_RegularArray_reduce_local_nextparents_64": ("awkward_RegularArray_reduce_local_nextparents_64.cpp", 14),
+    "awkward_RegularArray_reduce_nonlocal_preparenext_64": ("awkward_RegularArray_reduce_nonlocal_preparenext_64.cpp", 7),
+    "awkward_IndexedArray_reduce_next_64": ("awkward_IndexedArray_reduce_next_64.cpp", 7),
+    "awkward_IndexedArray_reduce_next_fix_offsets_64": ("awkward_IndexedArray_reduce_next_fix_offsets_64.cpp", 7),
+    "awkward_IndexedArray_reduce_next_nonlocal_nextshifts_64": ("awkward_IndexedArray_reduce_next_nonlocal_nextshifts_64.cpp", 7),
+    "awkward_IndexedArray_reduce_next_nonlocal_nextshifts_fromshifts_64": ("awkward_IndexedArray_reduce_next_nonlocal_nextshifts_fromshifts_64.cpp", 7),
+    "awkward_IndexedArray_local_preparenext_64": ("awkward_IndexedArray_local_preparenext_64.cpp", 7),
+    "awkward_ByteMaskedArray_reduce_next_64": ("awkward_ByteMaskedArray_reduce_next_64.cpp", 7),
+    "awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_64": ("awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_64.cpp", 7),
+    "awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_fromshifts_64": ("awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_fromshifts_64.cpp", 7),
 }
 
 _C_TYPES = {

@@ -38,6 +38,42 @@ extern "C" {
 #define AWKWARD_GB300_ERROR_BITS 8
 #define AWKWARD_GB300_NO_ERROR 0xffffffffffffffffULL
 
+/* ---- awkward_ByteMaskedArray_reduce_next_64: replaces awkward-cpp/src/cpu-kernels/awkward_ByteMaskedArray_reduce_next_64.cpp:7 */
+/* kernel-specification.yml:233 */
+int awkward_ByteMaskedArray_reduce_next_64(int64_t* nextcarry, int64_t* nextoffsets, int64_t* outindex, const int8_t* mask, const int64_t* offsets, int64_t outlength, bool validwhen, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_64: replaces awkward-cpp/src/cpu-kernels/awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_64.cpp:7 */
+/* kernel-specification.yml:261 */
+int awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_64(int64_t* nextshifts, const int8_t* mask, int64_t length, bool valid_when, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_fromshifts_64: replaces awkward-cpp/src/cpu-kernels/awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_fromshifts_64.cpp:7 */
+/* kernel-specification.yml:284 */
+int awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_fromshifts_64(int64_t* nextshifts, const int8_t* mask, int64_t length, bool valid_when, const int64_t* shifts, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_IndexedArray_local_preparenext_64: replaces awkward-cpp/src/cpu-kernels/awkward_IndexedArray_local_preparenext_64.cpp:7 */
+/* kernel-specification.yml:549 */
+int awkward_IndexedArray_local_preparenext_64(int64_t* tocarry, const int64_t* starts, const int64_t* offsets, const int64_t* nextoffsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_IndexedArray_reduce_next_64: replaces awkward-cpp/src/cpu-kernels/awkward_IndexedArray_reduce_next_64.cpp:7 */
+/* kernel-specification.yml:707 */
+int awkward_IndexedArray32_reduce_next_64(int64_t* nextcarry, int64_t* nextoffsets, int64_t* outindex, const int32_t* index, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:715 */
+int awkward_IndexedArray64_reduce_next_64(int64_t* nextcarry, int64_t* nextoffsets, int64_t* outindex, const int64_t* index, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:723 */
+int awkward_IndexedArrayU32_reduce_next_64(int64_t* nextcarry, int64_t* nextoffsets, int64_t* outindex, const uint32_t* index, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_IndexedArray_reduce_next_fix_offsets_64: replaces awkward-cpp/src/cpu-kernels/awkward_IndexedArray_reduce_next_fix_offsets_64.cpp:7 */
+/* kernel-specification.yml:750 */
+int awkward_IndexedArray_reduce_next_fix_offsets_64(int64_t* outoffsets, const int64_t* starts, int64_t startslength, int64_t outindexlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_IndexedArray_reduce_next_nonlocal_nextshifts_64: replaces awkward-cpp/src/cpu-kernels/awkward_IndexedArray_reduce_next_nonlocal_nextshifts_64.cpp:7 */
+/* kernel-specification.yml:799 */
+int awkward_IndexedArray32_reduce_next_nonlocal_nextshifts_64(int64_t* nextshifts, const int32_t* index, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:804 */
+int awkward_IndexedArray64_reduce_next_nonlocal_nextshifts_64(int64_t* nextshifts, const int64_t* index, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:809 */
+int awkward_IndexedArrayU32_reduce_next_nonlocal_nextshifts_64(int64_t* nextshifts, const uint32_t* index, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_IndexedArray_reduce_next_nonlocal_nextshifts_fromshifts_64: replaces awkward-cpp/src/cpu-kernels/awkward_IndexedArray_reduce_next_nonlocal_nextshifts_fromshifts_64.cpp:7 */
+/* kernel-specification.yml:829 */
+int awkward_IndexedArray32_reduce_next_nonlocal_nextshifts_fromshifts_64(int64_t* nextshifts, const int32_t* index, int64_t length, const int64_t* shifts, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:835 */
+int awkward_IndexedArray64_reduce_next_nonlocal_nextshifts_fromshifts_64(int64_t* nextshifts, const int64_t* index, int64_t length, const int64_t* shifts, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:841 */
+int awkward_IndexedArrayU32_reduce_next_nonlocal_nextshifts_fromshifts_64(int64_t* nextshifts, const uint32_t* index, int64_t length, const int64_t* shifts, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_ListArray_broadcast_tooffsets: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_broadcast_tooffsets.cpp:8 */
 /* kernel-specification.yml:1080 */
 int awkward_ListArray32_broadcast_tooffsets_64(int64_t* tocarry, const int64_t* fromoffsets, int64_t offsetslength, const int32_t* fromstarts, const int32_t* fromstops, int64_t lencontent, uint64_t invocation_index, uint64_t* err_code, void* stream);
@@ -110,6 +146,28 @@ int awkward_ListArray32_localindex_64(int64_t* toindex, const int32_t* offsets, 
 int awkward_ListArray64_localindex_64(int64_t* toindex, const int64_t* offsets, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* kernel-specification.yml:1931 */
 int awkward_ListArrayU32_localindex_64(int64_t* toindex, const uint32_t* offsets, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListOffsetArray_local_preparenext_64: replaces awkward-cpp/src/cpu-kernels/awkward_ListOffsetArray_local_preparenext_64.cpp:11 */
+/* kernel-specification.yml:2153 */
+int awkward_ListOffsetArray_local_preparenext_64(int64_t* tocarry, const int64_t* fromindex, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListOffsetArray_reduce_local_nextparents_64: replaces awkward-cpp/src/cpu-kernels/awkward_ListOffsetArray_reduce_local_nextparents_64.cpp:14 */
+/* kernel-specification.yml:2168 */
+int awkward_ListOffsetArray32_reduce_local_nextparents_64(int32_t* nextparents, const int32_t* offsets, int64_t length, int64_t nextparents_length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:2174 */
+int awkward_ListOffsetArray64_reduce_local_nextparents_64(int64_t* nextparents, const int64_t* offsets, int64_t length, int64_t nextparents_length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:2180 */
+int awkward_ListOffsetArrayU32_reduce_local_nextparents_64(uint32_t* nextparents, const uint32_t* offsets, int64_t length, int64_t nextparents_length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListOffsetArray_reduce_nonlocal_maxcount_offsetscopy_64: replaces awkward-cpp/src/cpu-kernels/awkward_ListOffsetArray_reduce_nonlocal_maxcount_offsetscopy_64.cpp:7 */
+/* kernel-specification.yml:2199 */
+int awkward_ListOffsetArray_reduce_nonlocal_maxcount_offsetscopy_64(int64_t* maxcount, int64_t* offsetscopy, const int64_t* offsets, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListOffsetArray_reduce_nonlocal_nextshifts_64: replaces awkward-cpp/src/cpu-kernels/awkward_ListOffsetArray_reduce_nonlocal_nextshifts_64.cpp:7 */
+/* kernel-specification.yml:2221 */
+int awkward_ListOffsetArray_reduce_nonlocal_nextshifts_64(int64_t* nummissing, int64_t* missing, int64_t* nextshifts, const int64_t* offsets, int64_t length, const int64_t* starts, const int64_t* outer_offsets, int64_t outlength, int64_t maxcount, int64_t nextlen, const int64_t* nextcarry, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListOffsetArray_reduce_nonlocal_outstartsstops_64: replaces awkward-cpp/src/cpu-kernels/awkward_ListOffsetArray_reduce_nonlocal_outstartsstops_64.cpp:10 */
+/* kernel-specification.yml:2258 */
+int awkward_ListOffsetArray_reduce_nonlocal_outstartsstops_64(int64_t* outstarts, int64_t* outstops, const int64_t* distincts, int64_t lendistincts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListOffsetArray_reduce_nonlocal_preparenext_64: replaces awkward-cpp/src/cpu-kernels/awkward_ListOffsetArray_reduce_nonlocal_preparenext_64.cpp:7 */
+/* kernel-specification.yml:2298 */
+int awkward_ListOffsetArray_reduce_nonlocal_preparenext_64(int64_t* nextcarry, int64_t* nextoffsets, int64_t nextlen, int64_t* maxnextparents, int64_t* distincts, int64_t distinctslen, int64_t* offsetscopy, const int64_t* offsets, int64_t length, const int64_t* outer_offsets, int64_t outlength, int64_t maxcount, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_NumpyArray_reduce_adjust_starts_64: replaces awkward-cpp/src/cpu-kernels/awkward_NumpyArray_reduce_adjust_starts_64.cpp:7 */
 /* kernel-specification.yml:2552 */
 int awkward_NumpyArray_reduce_adjust_starts_64(int64_t* toptr, int64_t outlength, const int64_t* offsets, const int64_t* starts, uint64_t invocation_index, uint64_t* err_code, void* stream);
@@ -125,6 +183,12 @@ int awkward_RegularArray_getitem_jagged_expand_64(int64_t* multistarts, int64_t*
 /* ---- awkward_RegularArray_getitem_next_range: replaces awkward-cpp/src/cpu-kernels/awkward_RegularArray_getitem_next_range.cpp:8 */
 /* kernel-specification.yml:3014 */
 int awkward_RegularArray_getitem_next_range_64(int64_t* tocarry, int64_t regular_start, int64_t step, int64_t length, int64_t size, int64_t nextsize, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_RegularArray_reduce_local_nextparents_64: replaces awkward-cpp/src/cpu-kernels/awkward_RegularArray_reduce_local_nextparents_64.cpp:14 */
+/* kernel-specification.yml:3067 */
+int awkward_RegularArray_reduce_local_nextparents_64(int64_t* nextparents, int64_t size, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_RegularArray_reduce_nonlocal_preparenext_64: replaces awkward-cpp/src/cpu-kernels/awkward_RegularArray_reduce_nonlocal_preparenext_64.cpp:7 */
+/* kernel-specification.yml:3085 */
+int awkward_RegularArray_reduce_nonlocal_preparenext_64(int64_t* nextcarry, int64_t* nextoffsets, const int64_t* offsets, int64_t size, int64_t length, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_argsort: replaces awkward-cpp/src/cpu-kernels/awkward_argsort.cpp:62 */
 /* kernel-specification.yml:3724 */
 int awkward_argsort_bool_int32(int64_t* toptr, const bool* fromptr, int64_t length, const int32_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);

@@ -800,6 +800,278 @@ ORACLE_SORT(awkward_sort_float32, float, oracle_less_float32)
 ORACLE_SORT(awkward_sort_float64, double, oracle_less_float64)
 
 /* ======================================================================
+ * Reductions above the innermost axis and through option types
+ * (awkward_ListOffsetArray_reduce_*, awkward_RegularArray_reduce_*,
+ *  awkward_IndexedArray_reduce_next*, awkward_ByteMaskedArray_reduce_next*)
+ * ====================================================================== */
+
+/* awkward_ListOffsetArray_reduce_nonlocal_maxcount_offsetscopy_64.cpp:7-21 */
+struct Error awkward_ListOffsetArray_reduce_nonlocal_maxcount_offsetscopy_64(
+    int64_t* maxcount, int64_t* offsetscopy, const int64_t* offsets, int64_t length) {
+  int64_t best = 0;
+  offsetscopy[0] = offsets[0];
+  for (int64_t i = 0; i < length; i++) {
+    if (offsets[i + 1] - offsets[i] > best) best = offsets[i + 1] - offsets[i];
+    offsetscopy[i + 1] = offsets[i + 1];
+  }
+  *maxcount = best;
+  return success();
+}
+
+/* awkward_ListOffsetArray_reduce_nonlocal_preparenext_64.cpp:7-57: the
+ * elements of the rows of each outer bin, column by column (bin-major), so
+ * next bin b*maxcount + col holds column `col` of every row of bin b that
+ * reaches it, rows in order. */
+struct Error awkward_ListOffsetArray_reduce_nonlocal_preparenext_64(
+    int64_t* nextcarry, int64_t* nextoffsets, int64_t nextlen, int64_t* maxnextparents,
+    int64_t* distincts, int64_t distinctslen, int64_t* offsetscopy, const int64_t* offsets,
+    int64_t length, const int64_t* outer_offsets, int64_t outlength, int64_t maxcount) {
+  (void)nextlen;
+  (void)offsetscopy;
+  (void)length;
+  *maxnextparents = -1;
+  for (int64_t i = 0; i < distinctslen; i++) distincts[i] = -1;
+  int64_t k = 0;
+  nextoffsets[0] = 0;
+  for (int64_t b = 0; b < outlength; b++) {
+    for (int64_t col = 0; col < maxcount; col++) {
+      const int64_t bin = b * maxcount + col;
+      const int64_t k0 = k;
+      for (int64_t row = outer_offsets[b]; row < outer_offsets[b + 1]; row++)
+        if (col < offsets[row + 1] - offsets[row]) nextcarry[k++] = offsets[row] + col;
+      nextoffsets[bin + 1] = k;
+      if (k > k0) {
+        if (bin < distinctslen) distincts[bin] = bin;
+        if (bin > *maxnextparents) *maxnextparents = bin;
+      }
+    }
+  }
+  return success();
+}
+
+/* awkward_ListOffsetArray_reduce_nonlocal_outstartsstops_64.cpp:10-44:
+ * sublist k of `distincts` is [k*maxcount, (k+1)*maxcount); it ends after
+ * its last entry that is not -1. */
+struct Error awkward_ListOffsetArray_reduce_nonlocal_outstartsstops_64(
+    int64_t* outstarts, int64_t* outstops, const int64_t* distincts, int64_t lendistincts,
+    int64_t outlength) {
+  if (outlength > 0 && lendistincts > 0) {
+    const int64_t maxcount = lendistincts / outlength;
+    int64_t k = 0, next = 0;
+    for (int64_t i = 0; i < lendistincts; i++) {
+      if (i == next) {
+        next += maxcount;
+        outstarts[k] = i;
+        outstops[k] = i;
+        k++;
+      }
+      if (distincts[i] != -1) outstops[k - 1] = i + 1;
+    }
+  } else {
+    for (int64_t k = 0; k < outlength; k++) outstarts[k] = outstops[k] = 0;
+  }
+  return success();
+}
+
+/* awkward_ListOffsetArray_reduce_nonlocal_nextshifts_64.cpp:7-43:
+ * missing[element (row, j)] = rows of the same outer bin up to `row` that
+ * end at or before column j; nextshifts gathers it through nextcarry. */
+struct Error awkward_ListOffsetArray_reduce_nonlocal_nextshifts_64(
+    int64_t* nummissing, int64_t* missing, int64_t* nextshifts, const int64_t* offsets,
+    int64_t length, const int64_t* starts, const int64_t* outer_offsets, int64_t outlength,
+    int64_t maxcount, int64_t nextlen, const int64_t* nextcarry) {
+  (void)length;
+  (void)starts;
+  for (int64_t b = 0; b < outlength; b++) {
+    for (int64_t c = 0; c < maxcount; c++) nummissing[c] = 0;
+    for (int64_t row = outer_offsets[b]; row < outer_offsets[b + 1]; row++) {
+      const int64_t start = offsets[row], count = offsets[row + 1] - offsets[row];
+      for (int64_t c = count; c < maxcount; c++) nummissing[c]++;
+      for (int64_t j = 0; j < count; j++) missing[start + j] = nummissing[j];
+    }
+  }
+  for (int64_t j = 0; j < nextlen; j++) nextshifts[j] = missing[nextcarry[j]];
+  return success();
+}
+
+/* awkward_ListOffsetArray_reduce_local_nextparents_64.cpp:14-27 */
+#define ORACLE_LOCAL_NEXTPARENTS(NAME, C)                                      \
+  struct Error NAME(C* nextparents, const C* offsets, int64_t length,          \
+                    int64_t nextparents_length) {                              \
+    const int64_t base = (int64_t)offsets[0];                                  \
+    for (int64_t i = 0; i < length; i++)                                       \
+      for (int64_t j = (int64_t)offsets[i] - base;                             \
+           j < (int64_t)offsets[i + 1] - base && j < nextparents_length; j++)  \
+        nextparents[j] = (C)i;                                                 \
+    return success();                                                          \
+  }
+ORACLE_LOCAL_NEXTPARENTS(awkward_ListOffsetArray32_reduce_local_nextparents_64, int32_t)
+ORACLE_LOCAL_NEXTPARENTS(awkward_ListOffsetArrayU32_reduce_local_nextparents_64, uint32_t)
+ORACLE_LOCAL_NEXTPARENTS(awkward_ListOffsetArray64_reduce_local_nextparents_64, int64_t)
+
+/* awkward_ListOffsetArray_local_preparenext_64.cpp:11-26: the permutation
+ * that orders `fromindex` (ties, which the CPU leaves in std::sort's order,
+ * are kept in index order here). */
+struct Error awkward_ListOffsetArray_local_preparenext_64(int64_t* tocarry,
+                                                          const int64_t* fromindex,
+                                                          int64_t length) {
+  for (int64_t i = 0; i < length; i++) tocarry[i] = i;
+  oracle_stable_sort(tocarry, length, fromindex, oracle_less_int64, 1);
+  return success();
+}
+
+/* awkward_RegularArray_reduce_local_nextparents_64.cpp:14-26 */
+struct Error awkward_RegularArray_reduce_local_nextparents_64(int64_t* nextparents, int64_t size,
+                                                              int64_t length) {
+  int64_t k = 0;
+  for (int64_t i = 0; i < length; i++)
+    for (int64_t j = 0; j < size; j++) nextparents[k++] = i;
+  return success();
+}
+
+/* awkward_RegularArray_reduce_nonlocal_preparenext_64.cpp:7-36 */
+struct Error awkward_RegularArray_reduce_nonlocal_preparenext_64(
+    int64_t* nextcarry, int64_t* nextoffsets, const int64_t* offsets, int64_t size,
+    int64_t length, int64_t outlength) {
+  (void)length;
+  int64_t k = 0;
+  nextoffsets[0] = 0;
+  for (int64_t b = 0; b < outlength; b++) {
+    for (int64_t j = 0; j < size; j++) {
+      for (int64_t i = offsets[b]; i < offsets[b + 1]; i++) nextcarry[k++] = i * size + j;
+      nextoffsets[b * size + j + 1] = k;
+    }
+  }
+  return success();
+}
+
+/* awkward_IndexedArray_reduce_next_64.cpp:7-30: compact the non-missing
+ * entries of each bin. */
+#define ORACLE_INDEXED_REDUCE_NEXT(NAME, T)                                    \
+  struct Error NAME(int64_t* nextcarry, int64_t* nextoffsets, int64_t* outindex, \
+                    const T* index, const int64_t* offsets, int64_t outlength) { \
+    int64_t k = 0;                                                             \
+    nextoffsets[0] = 0;                                                        \
+    for (int64_t b = 0; b < outlength; b++) {                                  \
+      for (int64_t i = offsets[b]; i < offsets[b + 1]; i++) {                  \
+        if ((int64_t)index[i] >= 0) {                                          \
+          nextcarry[k] = (int64_t)index[i];                                    \
+          outindex[i] = k++;                                                   \
+        } else {                                                               \
+          outindex[i] = -1;                                                    \
+        }                                                                      \
+      }                                                                        \
+      nextoffsets[b + 1] = k;                                                  \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_INDEXED_REDUCE_NEXT(awkward_IndexedArray32_reduce_next_64, int32_t)
+ORACLE_INDEXED_REDUCE_NEXT(awkward_IndexedArrayU32_reduce_next_64, uint32_t)
+ORACLE_INDEXED_REDUCE_NEXT(awkward_IndexedArray64_reduce_next_64, int64_t)
+
+/* awkward_IndexedArray_reduce_next_fix_offsets_64.cpp:7-17 */
+struct Error awkward_IndexedArray_reduce_next_fix_offsets_64(int64_t* outoffsets,
+                                                             const int64_t* starts,
+                                                             int64_t startslength,
+                                                             int64_t outindexlength) {
+  for (int64_t i = 0; i < startslength; i++) outoffsets[i] = starts[i];
+  outoffsets[startslength] = outindexlength;
+  return success();
+}
+
+/* awkward_IndexedArray_reduce_next_nonlocal_nextshifts_64.cpp:7-24 and
+ * ..._fromshifts_64.cpp:7-25: for the k-th non-missing entry i, the number
+ * of missing entries before it (plus shifts[i]). */
+#define ORACLE_INDEXED_NEXTSHIFTS(NAME, T)                                     \
+  struct Error NAME(int64_t* nextshifts, const T* index, int64_t length) {     \
+    int64_t k = 0;                                                             \
+    for (int64_t i = 0; i < length; i++)                                       \
+      if ((int64_t)index[i] >= 0) {                                            \
+        nextshifts[k] = i - k;                                                 \
+        k++;                                                                   \
+      }                                                                        \
+    return success();                                                          \
+  }
+#define ORACLE_INDEXED_NEXTSHIFTS_FROM(NAME, T)                                \
+  struct Error NAME(int64_t* nextshifts, const T* index, int64_t length,       \
+                    const int64_t* shifts) {                                   \
+    int64_t k = 0;                                                             \
+    for (int64_t i = 0; i < length; i++)                                       \
+      if ((int64_t)index[i] >= 0) {                                            \
+        nextshifts[k] = shifts[i] + (i - k);                                   \
+        k++;                                                                   \
+      }                                                                        \
+    return success();                                                          \
+  }
+ORACLE_INDEXED_NEXTSHIFTS(awkward_IndexedArray32_reduce_next_nonlocal_nextshifts_64, int32_t)
+ORACLE_INDEXED_NEXTSHIFTS(awkward_IndexedArrayU32_reduce_next_nonlocal_nextshifts_64, uint32_t)
+ORACLE_INDEXED_NEXTSHIFTS(awkward_IndexedArray64_reduce_next_nonlocal_nextshifts_64, int64_t)
+ORACLE_INDEXED_NEXTSHIFTS_FROM(awkward_IndexedArray32_reduce_next_nonlocal_nextshifts_fromshifts_64, int32_t)
+ORACLE_INDEXED_NEXTSHIFTS_FROM(awkward_IndexedArrayU32_reduce_next_nonlocal_nextshifts_fromshifts_64, uint32_t)
+ORACLE_INDEXED_NEXTSHIFTS_FROM(awkward_IndexedArray64_reduce_next_nonlocal_nextshifts_fromshifts_64, int64_t)
+
+/* awkward_IndexedArray_local_preparenext_64.cpp:7-31 */
+struct Error awkward_IndexedArray_local_preparenext_64(int64_t* tocarry, const int64_t* starts,
+                                                       const int64_t* offsets,
+                                                       const int64_t* nextoffsets,
+                                                       int64_t outlength) {
+  (void)starts;
+  for (int64_t b = 0; b < outlength; b++) {
+    int64_t k = nextoffsets[b];
+    for (int64_t i = offsets[b]; i < offsets[b + 1]; i++)
+      tocarry[i] = k < nextoffsets[b + 1] ? k++ : -1;
+  }
+  return success();
+}
+
+/* awkward_ByteMaskedArray_reduce_next_64.cpp:7-32 */
+struct Error awkward_ByteMaskedArray_reduce_next_64(int64_t* nextcarry, int64_t* nextoffsets,
+                                                    int64_t* outindex, const int8_t* mask,
+                                                    const int64_t* offsets, int64_t outlength,
+                                                    bool validwhen) {
+  int64_t k = 0;
+  nextoffsets[0] = 0;
+  for (int64_t b = 0; b < outlength; b++) {
+    for (int64_t i = offsets[b]; i < offsets[b + 1]; i++) {
+      if ((mask[i] != 0) == validwhen) {
+        nextcarry[k] = i;
+        outindex[i] = k++;
+      } else {
+        outindex[i] = -1;
+      }
+    }
+    nextoffsets[b + 1] = k;
+  }
+  return success();
+}
+
+/* awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_64.cpp:7-25 and
+ * ..._fromshifts_64.cpp:7-26 */
+struct Error awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_64(int64_t* nextshifts,
+                                                                        const int8_t* mask,
+                                                                        int64_t length,
+                                                                        bool valid_when) {
+  int64_t k = 0;
+  for (int64_t i = 0; i < length; i++)
+    if ((mask[i] != 0) == valid_when) {
+      nextshifts[k] = i - k;
+      k++;
+    }
+  return success();
+}
+struct Error awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_fromshifts_64(
+    int64_t* nextshifts, const int8_t* mask, int64_t length, bool valid_when,
+    const int64_t* shifts) {
+  int64_t k = 0;
+  for (int64_t i = 0; i < length; i++)
+    if ((mask[i] != 0) == valid_when) {
+      nextshifts[k] = shifts[i] + (i - k);
+      k++;
+    }
+  return success();
+}
+
+/* ======================================================================
  * Multi-core driver for the CPU baseline: run one reducer (any of the
  * (toptr, fromptr, offsets, outlength) family above, or argmax/argmin with
  * `starts`) over `nthreads` contiguous list ranges.  Each thread calls the

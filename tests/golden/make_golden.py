@@ -319,6 +319,140 @@ def sort_cases(rng, name):
     return out
 
 
+def _two_level(rng, nbins, lam_rows, lam_len, longs=(), p_empty_bin=0.1):
+    """Outer bins of rows and rows of elements: (outer_offsets, offsets, L)."""
+    R = rng.poisson(lam_rows, nbins).astype(np.int64)
+    R[rng.random(nbins) < p_empty_bin] = 0
+    outer = _offsets(R)
+    L = _lengths(rng, int(outer[-1]), lam_len, p_empty=0.1, longs=longs)
+    return outer, _offsets(L), L
+
+
+def nonlocal_cases(rng, name):
+    """Seeded inputs of the non-local / option-type reduction kernels."""
+    rec = SIGNATURES[name]
+    fam = rec["family"]
+    args = {a[0]: a for a in rec["args"]}
+    out = []
+    S = 777  # untouched output slots keep this value
+    if fam == "awkward_ListOffsetArray_reduce_nonlocal_maxcount_offsetscopy_64":
+        for n in (0, 1, 150):
+            off = _offsets(_lengths(rng, n, 5, longs=(40,)))
+            out.append({"maxcount": np.full(1, S, np.int64), "offsetscopy": np.full(n + 1, S, np.int64),
+                        "offsets": off, "length": n})
+    elif fam in ("awkward_ListOffsetArray_reduce_nonlocal_preparenext_64",
+                 "awkward_ListOffsetArray_reduce_nonlocal_nextshifts_64"):
+        ref = oracle.load()
+        for nbins, lr, ll, longs in ((1, 60, 4, ()), (40, 3, 3, ()), (25, 4, 2, (30,)), (0, 1, 1, ())):
+            outer, off, L = _two_level(rng, nbins, lr, ll, longs)
+            nrows = len(L)
+            M = int(L.max()) if nrows else 0
+            E = int(off[-1])
+            nbinsM = nbins * M
+            prep = {"nextcarry": np.full(E, S, np.int64), "nextoffsets": np.full(nbinsM + 1, S, np.int64),
+                    "nextlen": E, "maxnextparents": np.full(1, S, np.int64),
+                    "distincts": np.full(nbinsM, S, np.int64), "distinctslen": nbinsM,
+                    "offsetscopy": np.full(nrows + 1, S, np.int64), "offsets": off, "length": nrows,
+                    "outer_offsets": outer, "outlength": nbins, "maxcount": M}
+            if fam.endswith("preparenext_64"):
+                out.append(prep)
+                continue
+            kw = {k: (v.copy() if isinstance(v, np.ndarray) else v) for k, v in prep.items()}
+            oracle.call(ref, "awkward_ListOffsetArray_reduce_nonlocal_preparenext_64", **kw)
+            out.append({"nummissing": np.full(max(M, 1), S, np.int64), "missing": np.full(E, S, np.int64),
+                        "nextshifts": np.full(E, S, np.int64), "offsets": off, "length": nrows,
+                        "starts": off[:-1].copy(), "outer_offsets": outer, "outlength": nbins,
+                        "maxcount": M, "nextlen": E, "nextcarry": kw["nextcarry"]})
+    elif fam == "awkward_ListOffsetArray_reduce_nonlocal_outstartsstops_64":
+        for outlength, M in ((0, 3), (3, 0), (1, 7), (30, 5), (12, 1)):
+            n = outlength * M
+            d = np.where(rng.random(n) < 0.4, -1, rng.integers(0, 50, n)).astype(np.int64)
+            d[: M] = -1  # one sublist without any entry
+            out.append({"outstarts": np.full(outlength, S, np.int64), "outstops": np.full(outlength, S, np.int64),
+                        "distincts": d, "lendistincts": n, "outlength": outlength})
+    elif fam == "awkward_ListOffsetArray_reduce_local_nextparents_64":
+        C = NP_DTYPES[args["offsets"][1]]
+        for n, first, trim in ((0, 0, 0), (120, 0, 0), (90, 17, 0), (80, 5, 30)):
+            off = _offsets(_lengths(rng, n, 4, longs=(33,))) + first
+            E = int(off[-1] - off[0])
+            out.append({"nextparents": np.full(E, S, C), "offsets": off.astype(C), "length": n,
+                        "nextparents_length": max(E - trim, 0)})
+    elif fam == "awkward_ListOffsetArray_local_preparenext_64":
+        for n in (0, 1, 300):
+            out.append({"tocarry": np.full(n, S, np.int64),
+                        "fromindex": rng.permutation(3 * n)[:n].astype(np.int64), "length": n})
+    elif fam == "awkward_RegularArray_reduce_local_nextparents_64":
+        for size, length in ((0, 5), (3, 0), (4, 37), (1, 10)):
+            out.append({"nextparents": np.full(size * length, S, np.int64), "size": size, "length": length})
+    elif fam == "awkward_RegularArray_reduce_nonlocal_preparenext_64":
+        for nbins, size in ((0, 3), (1, 4), (20, 3), (15, 0), (9, 1)):
+            R = rng.poisson(3, nbins).astype(np.int64)
+            R[rng.random(nbins) < 0.15] = 0
+            off = _offsets(R)
+            rows = int(off[-1])
+            out.append({"nextcarry": np.full(rows * size, S, np.int64),
+                        "nextoffsets": np.full(nbins * size + 1, S, np.int64), "offsets": off,
+                        "size": size, "length": rows, "outlength": nbins})
+    elif fam == "awkward_IndexedArray_reduce_next_64":
+        T = NP_DTYPES[args["index"][1]]
+        for nbins in (0, 1, 60):
+            off = _offsets(_lengths(rng, nbins, 4, p_empty=0.15, longs=(40,)))
+            E = int(off[-1])
+            idx = rng.integers(0, 1000, E)
+            if T != np.uint32:
+                idx[rng.random(E) < 0.25] = -1
+            out.append({"nextcarry": np.full(E, S, np.int64), "nextoffsets": np.full(nbins + 1, S, np.int64),
+                        "outindex": np.full(E, S, np.int64), "index": idx.astype(T), "offsets": off,
+                        "outlength": nbins})
+    elif fam == "awkward_IndexedArray_reduce_next_fix_offsets_64":
+        for n in (0, 1, 50):
+            st = np.sort(rng.integers(0, 500, n)).astype(np.int64)
+            out.append({"outoffsets": np.full(n + 1, S, np.int64), "starts": st, "startslength": n,
+                        "outindexlength": 500 + n})
+    elif fam in ("awkward_IndexedArray_reduce_next_nonlocal_nextshifts_64",
+                 "awkward_IndexedArray_reduce_next_nonlocal_nextshifts_fromshifts_64"):
+        T = NP_DTYPES[args["index"][1]]
+        for n in (0, 1, 400):
+            idx = rng.integers(0, 1000, n)
+            if T != np.uint32:
+                idx[rng.random(n) < 0.3] = -1
+            kw = {"nextshifts": np.full(n, S, np.int64), "index": idx.astype(T), "length": n}
+            if "shifts" in args:
+                kw["shifts"] = rng.integers(0, 20, n).astype(np.int64)
+            out.append(kw)
+    elif fam == "awkward_IndexedArray_local_preparenext_64":
+        for nbins in (0, 1, 70):
+            Lo = _lengths(rng, nbins, 4, p_empty=0.15, longs=(40,))
+            off = _offsets(Lo)
+            Li = np.array([rng.integers(0, x + 1) for x in Lo], np.int64)
+            out.append({"tocarry": np.full(int(off[-1]), S, np.int64), "starts": off[:-1].copy(),
+                        "offsets": off, "nextoffsets": _offsets(Li), "outlength": nbins})
+    elif fam == "awkward_ByteMaskedArray_reduce_next_64":
+        for nbins, vw in ((0, True), (1, False), (60, True), (45, False)):
+            off = _offsets(_lengths(rng, nbins, 4, p_empty=0.15, longs=(40,)))
+            E = int(off[-1])
+            m = (rng.random(E) < 0.6).astype(np.int8) * rng.integers(1, 5, E).astype(np.int8)
+            out.append({"nextcarry": np.full(E, S, np.int64), "nextoffsets": np.full(nbins + 1, S, np.int64),
+                        "outindex": np.full(E, S, np.int64), "mask": m, "offsets": off,
+                        "outlength": nbins, "validwhen": vw})
+    elif fam in ("awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_64",
+                 "awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_fromshifts_64"):
+        for n, vw in ((0, True), (1, True), (300, True), (300, False)):
+            m = (rng.random(n) < 0.6).astype(np.int8)
+            kw = {"nextshifts": np.full(n, S, np.int64), "mask": m, "length": n, "valid_when": vw}
+            if "shifts" in args:
+                kw["shifts"] = rng.integers(0, 20, n).astype(np.int64)
+            out.append(kw)
+    else:
+        raise KeyError(fam)
+    return out
+
+
+NONLOCAL_PREFIXES = ("awkward_ListOffsetArray_reduce_", "awkward_ListOffsetArray_local_",
+                     "awkward_RegularArray_reduce_", "awkward_IndexedArray_",
+                     "awkward_ByteMaskedArray_")
+
+
 def make_random():
     ref = oracle.load_ref()
     ref = oracle.load_ref()
@@ -332,6 +466,8 @@ def make_random():
         rng = np.random.default_rng([20241203, zlib.crc32(name.encode())])
         if fam in ("awkward_argsort", "awkward_sort"):
             cases = sort_cases(rng, name)
+        elif fam.startswith(NONLOCAL_PREFIXES):
+            cases = nonlocal_cases(rng, name)
         elif fam == "awkward_RegularArray_combinations_64":
             cases = regular_combinations_cases(rng, name)
         elif fam == "awkward_ListArray_broadcast_tooffsets":
