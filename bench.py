@@ -479,6 +479,111 @@ def measure_c5(dev, reps, warmup, n_lists=4_000_000):
     return res
 
 
+def measure_sort(be, dev, reps, warmup, n_lists=10_000_000):
+    """ak.argsort / ak.sort(axis=-1) on float64: the C1 shape (10M lists of
+    Poisson(8)) and a wide shape (2,000 lists of Poisson(40,000), the merged
+    path for segments past 2048).  Device time per call, inputs resident;
+    algorithmic bytes 8E read + 8(N+1) offsets + 8E written."""
+    import torch
+
+    res = {}
+    stream = torch.cuda.current_stream(dev)
+    for tag, nl, lam in (("c1_shape", n_lists, 8.0), ("wide", max(n_lists // 5000, 1), 40_000.0)):
+        gen = torch.Generator(device=dev).manual_seed(11)
+        L = torch.poisson(torch.full((nl,), lam, device=dev), generator=gen).to(torch.int64)
+        off = torch.zeros(nl + 1, dtype=torch.int64, device=dev)
+        torch.cumsum(L, 0, out=off[1:])
+        E = int(off[-1].item())
+        x = torch.randn(E, dtype=torch.float64, device=dev, generator=gen)
+        idx = torch.empty(E, dtype=torch.int64, device=dev)
+        srt = torch.empty(E, dtype=torch.float64, device=dev)
+        k_arg = be.by_name("awkward_argsort_float64_int64")
+        k_srt = be.by_name("awkward_sort_float64")
+        for _ in range(max(warmup, 3)):
+            k_arg(idx, x, E, off, nl + 1, True, True)
+            k_srt(srt, x, E, off, nl + 1, True, True)
+        be.synchronize()
+        t_arg = _time_ms(lambda: k_arg(idx, x, E, off, nl + 1, True, True), reps, stream)
+        t_srt = _time_ms(lambda: k_srt(srt, x, E, off, nl + 1, True, True), reps, stream)
+        be.synchronize()
+        nbytes = 16 * E + 8 * (nl + 1)
+        res[tag] = {"lists": nl, "elements": E, "argsort_ms": round(t_arg, 4),
+                    "sort_ms": round(t_srt, 4),
+                    "argsort_gelem_s": round(E / (t_arg * 1e-3) / 1e9, 2),
+                    "argsort_gbs": round(nbytes / (t_arg * 1e-3) / 1e9, 1)}
+        del x, idx, srt
+    return res
+
+
+def measure_nonlocal(be, dev, reps, warmup, n_rows=10_000_000):
+    """Reductions above the innermost axis, the kernel sequence awkward runs
+    (listoffsetarray.py _reduce_next, non-local branch): maxcount_offsetscopy,
+    preparenext, the content carry, the segmented sum over the next offsets and
+    outstartsstops.  axis0: ak.sum(x, axis=0) of 10M rows of Poisson(8)
+    float64 (one outer bin); axis1: ak.sum(x, axis=1) of a 3-level array, 1M
+    outer lists of Poisson(8) rows of Poisson(4).  Device time of the whole
+    sequence including its host reads of the sizes; elements/s."""
+    import torch
+
+    from awkward_gb300 import _abi
+
+    f_take = _abi.ext_cfunc("awkward_gb300_take")
+    k_mc = be.by_name("awkward_ListOffsetArray_reduce_nonlocal_maxcount_offsetscopy_64")
+    k_pn = be.by_name("awkward_ListOffsetArray_reduce_nonlocal_preparenext_64")
+    k_os = be.by_name("awkward_ListOffsetArray_reduce_nonlocal_outstartsstops_64")
+    k_sum = be["awkward_reduce_sum", np.float64, np.float64, np.int64]
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+    res = {}
+    for tag, nbins, lam_rows, lam_len in (("axis0", 1, None, 8.0),
+                                          ("axis1", max(n_rows // 10, 1), 8.0, 4.0)):
+        gen = torch.Generator(device=dev).manual_seed(13)
+        if lam_rows is None:
+            R = torch.full((1,), n_rows, dtype=torch.int64, device=dev)
+        else:
+            R = torch.poisson(torch.full((nbins,), lam_rows, device=dev), generator=gen).to(torch.int64)
+        outer = torch.zeros(nbins + 1, dtype=torch.int64, device=dev)
+        torch.cumsum(R, 0, out=outer[1:])
+        nrows = int(outer[-1].item())
+        L = torch.poisson(torch.full((nrows,), lam_len, device=dev), generator=gen).to(torch.int64)
+        off = torch.zeros(nrows + 1, dtype=torch.int64, device=dev)
+        torch.cumsum(L, 0, out=off[1:])
+        E = int(off[-1].item())
+        x = torch.randn(E, dtype=torch.float64, device=dev, generator=gen)
+        mc = torch.empty(1, dtype=torch.int64, device=dev)
+        ocopy = torch.empty(nrows + 1, dtype=torch.int64, device=dev)
+        k_mc(mc, ocopy, off, nrows)
+        be.synchronize()
+        M = int(mc.item())
+        nb = nbins * M
+        carry = torch.empty(E, dtype=torch.int64, device=dev)
+        noff = torch.empty(nb + 1, dtype=torch.int64, device=dev)
+        mnp = torch.empty(1, dtype=torch.int64, device=dev)
+        dist = torch.empty(nb, dtype=torch.int64, device=dev)
+        nxt = torch.empty(E, dtype=torch.float64, device=dev)
+        out = torch.empty(nb, dtype=torch.float64, device=dev)
+        ost = torch.empty(nbins, dtype=torch.int64, device=dev)
+        osp = torch.empty(nbins, dtype=torch.int64, device=dev)
+        err = torch.full((1,), -1, dtype=torch.int64, device=dev)
+
+        def chain():
+            k_mc(mc, ocopy, off, nrows)
+            k_pn(carry, noff, E, mnp, dist, nb, ocopy, off, nrows, outer, nbins, M)
+            f_take(nxt.data_ptr(), x.data_ptr(), 8, carry.data_ptr(), E, E, 0, err.data_ptr(), sp)
+            k_sum(out, nxt, noff, nb)
+            k_os(ost, osp, dist, nb, nbins)
+
+        for _ in range(max(warmup, 3)):
+            chain()
+        be.synchronize()
+        t = _time_ms(chain, reps, stream)
+        be.synchronize()
+        res[tag] = {"outer_bins": nbins, "rows": nrows, "elements": E, "maxcount": M,
+                    "chain_ms": round(t, 4), "gelem_s": round(E / (t * 1e-3) / 1e9, 2)}
+        del x, carry, nxt
+    return res
+
+
 def run_gb300(args):
     import torch
 
@@ -497,6 +602,14 @@ def run_gb300(args):
     if args.only == "c5":
         print(json.dumps({"c5_autograd": measure_c5(dev, args.steps, args.warmup,
                                                     args.lists or 4_000_000)}))
+        return
+    if args.only == "sort":
+        print(json.dumps({"sort": measure_sort(be, dev, args.steps, args.warmup,
+                                               args.lists or 10_000_000)}))
+        return
+    if args.only == "nonlocal":
+        print(json.dumps({"nonlocal_reduce": measure_nonlocal(be, dev, args.steps, args.warmup,
+                                                              args.lists or 10_000_000)}))
         return
     if args.only == "c3":
         n2 = args.lists or 5_000_000
@@ -625,6 +738,8 @@ def run_gb300(args):
         line["c2_jagged_slicing"] = measure_c2(be, dev, max(args.steps // 2, 5), args.warmup)
         line["c5_autograd"] = measure_c5(dev, max(args.steps // 2, 5), args.warmup)
         line["c4_batched"] = measure_c4(dev)
+        line["sort"] = measure_sort(be, dev, max(args.steps // 2, 5), args.warmup)
+        line["nonlocal_reduce"] = measure_nonlocal(be, dev, max(args.steps // 2, 5), args.warmup)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = {k: v for k, v in cpu_baseline(2_000_000, 1, 8.0).items()
                                 if k != "ms_per_step"}
@@ -647,7 +762,7 @@ def main():
                    help="list chunks of the host-buffer (e2e) pipeline")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the secondary workloads (combinations, ...)")
-    p.add_argument("--only", default=None, choices=["c2", "c3", "c4", "c5"],
+    p.add_argument("--only", default=None, choices=["c2", "c3", "c4", "c5", "sort", "nonlocal"],
                    help="run one secondary workload alone (profiling); --lists sets its size")
     p.add_argument("--lists", type=int, default=None,
                    help="list count (default: 10M lists for the reducers, 5M for --only c3; "
