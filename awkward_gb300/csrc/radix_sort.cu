@@ -2,17 +2,19 @@
 // exclusive scan and a lower-bound fill (see radix_sort.cuh).
 //
 // A pass sorts by one 8-bit digit in three launches:
-//   upsweep    each tile of 4096 pairs counts its digits (warp-aggregated
+//   upsweep    each tile of 2048 pairs counts its digits (warp-aggregated
 //              shared-memory atomics) into counts[digit][tile];
 //   scan       one exclusive scan over the digit-major counts gives every
 //              (digit, tile) its first output position;
-//   downsweep  each warp owns 512 consecutive pairs of its tile, 32 per step:
+//   downsweep  each warp owns 256 consecutive pairs of its tile, 32 per step:
 //              lanes holding the same digit find each other with
 //              __match_any_sync, rank among themselves by lane order and add
 //              to the warp's running count of that digit; the warps' counts
 //              are then scanned in warp order.  The rank of a pair is thus its
 //              order among equal digits in the input -- the pass is stable,
-//              and so is the whole least-significant-digit-first sort.
+//              and so is the whole least-significant-digit-first sort.  The
+//              tile is laid out in digit order in shared memory first, so the
+//              global stores of each digit's run are contiguous.
 #include "radix_sort.cuh"
 
 namespace gb {
@@ -20,9 +22,9 @@ namespace {
 
 constexpr int kRBlock = 256;
 constexpr int kRWarps = kRBlock / 32;
-constexpr int kRSteps = 16;                       // steps of 32 pairs per warp
-constexpr int kRTile = kRBlock * kRSteps;         // 4096 pairs per tile
-constexpr int kRWarpSpan = kRTile / kRWarps;      // 512 consecutive pairs per warp
+constexpr int kRSteps = 8;                        // steps of 32 pairs per warp
+constexpr int kRTile = kRBlock * kRSteps;         // 2048 pairs per tile
+constexpr int kRWarpSpan = kRTile / kRWarps;      // 256 consecutive pairs per warp
 constexpr int kRDigits = 256;
 
 __device__ __forceinline__ unsigned lanemask_lt() {
@@ -40,7 +42,7 @@ __global__ void __launch_bounds__(kRBlock)
   const long long tile = blockIdx.x;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const long long e0 = tile * kRTile + (long long)warp * kRWarpSpan;
-#pragma unroll 4
+#pragma unroll
   for (int j = 0; j < kRSteps; j++) {
     const long long e = e0 + j * 32 + lane;
     const bool valid = e < n;
@@ -52,25 +54,34 @@ __global__ void __launch_bounds__(kRBlock)
   for (int b = threadIdx.x; b <= (int)mask; b += kRBlock) counts[(long long)b * ntiles + tile] = h[b];
 }
 
+// Rank every pair of the tile among equal digits (warp-ordered counters, so
+// input order is kept), place the tile in shared memory in digit order, then
+// write each digit's run to its global position: consecutive threads store
+// consecutive positions of the same digit run.
 __global__ void __launch_bounds__(kRBlock)
     radix_downsweep(const unsigned long long* __restrict__ kin, const long long* __restrict__ vin,
                     unsigned long long* __restrict__ kout, long long* __restrict__ vout,
                     long long n, int shift, unsigned mask, const long long* __restrict__ starts,
                     long long ntiles) {
   __shared__ unsigned wcnt[kRWarps][kRDigits];
-  __shared__ long long gbase[kRDigits];
+  __shared__ unsigned s_tstart[kRDigits];       // first tile slot of each digit
+  __shared__ long long s_gbase[kRDigits];       // first global position of each digit (this tile)
+  __shared__ unsigned long long s_key[kRTile];
+  __shared__ unsigned short s_src[kRTile];      // tile position the slot's pair came from
+  __shared__ unsigned s_scan[kRBlock / 32 + 1];
   const long long tile = blockIdx.x;
+  const long long t0 = tile * kRTile;
   for (int i = threadIdx.x; i < kRWarps * kRDigits; i += kRBlock) (&wcnt[0][0])[i] = 0;
-  for (int b = threadIdx.x; b <= (int)mask; b += kRBlock) gbase[b] = starts[(long long)b * ntiles + tile];
+  for (int b = threadIdx.x; b <= (int)mask; b += kRBlock) s_gbase[b] = starts[(long long)b * ntiles + tile];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long e0 = tile * kRTile + (long long)warp * kRWarpSpan;
+  const int w0 = warp * kRWarpSpan;
   unsigned long long key[kRSteps];
   unsigned rank[kRSteps];
   const unsigned lt = lanemask_lt();
 #pragma unroll
   for (int j = 0; j < kRSteps; j++) {
-    const long long e = e0 + j * 32 + lane;
+    const long long e = t0 + w0 + j * 32 + lane;
     const bool valid = e < n;
     key[j] = valid ? kin[e] : 0ull;
     const unsigned d = valid ? (unsigned)(key[j] >> shift) & mask : 0xffffffffu;
@@ -83,25 +94,41 @@ __global__ void __launch_bounds__(kRBlock)
     __syncwarp();
   }
   __syncthreads();
-  for (int b = threadIdx.x; b <= (int)mask; b += kRBlock) {
+  // per digit: warps' counts -> exclusive warp offsets and the digit's tile total
+  unsigned dtot = 0;
+  for (int b = threadIdx.x; b < kRDigits; b += kRBlock) {
     unsigned run = 0;
 #pragma unroll
     for (int w = 0; w < kRWarps; w++) {
-      const unsigned c = wcnt[w][b];
-      wcnt[w][b] = run;
+      const unsigned c = b <= (int)mask ? wcnt[w][b] : 0u;
+      if (b <= (int)mask) wcnt[w][b] = run;
       run += c;
     }
+    dtot = run;  // kRBlock == kRDigits: one digit per thread
   }
+  unsigned total;
+  auto add = [](unsigned a, unsigned b) { return a + b; };
+  const unsigned dstart = block_exclusive_scan<kRBlock>(dtot, add, 0u, s_scan, &total);
+  s_tstart[threadIdx.x] = dstart;
   __syncthreads();
 #pragma unroll
   for (int j = 0; j < kRSteps; j++) {
-    const long long e = e0 + j * 32 + lane;
-    if (e < n) {
+    const int te = w0 + j * 32 + lane;
+    if (t0 + te < n) {
       const unsigned d = (unsigned)(key[j] >> shift) & mask;
-      const long long pos = gbase[d] + wcnt[warp][d] + rank[j];
-      kout[pos] = key[j];
-      vout[pos] = vin[e];
+      const unsigned slot = s_tstart[d] + wcnt[warp][d] + rank[j];
+      s_key[slot] = key[j];
+      s_src[slot] = (unsigned short)te;
     }
+  }
+  __syncthreads();
+  const int cnt = (int)(n - t0 < kRTile ? n - t0 : kRTile);
+  for (int i = threadIdx.x; i < cnt; i += kRBlock) {
+    const unsigned long long k = s_key[i];
+    const unsigned d = (unsigned)(k >> shift) & mask;
+    const long long pos = s_gbase[d] + (i - (long long)s_tstart[d]);
+    kout[pos] = k;
+    vout[pos] = vin[t0 + s_src[i]];
   }
 }
 
