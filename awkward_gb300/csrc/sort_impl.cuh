@@ -35,6 +35,7 @@
 #include <type_traits>
 
 #include "gb_common.cuh"
+#include "radix_sort.cuh"
 
 using namespace gb;
 
@@ -406,17 +407,48 @@ __device__ __forceinline__ long long merge_split_g(const unsigned long long* ak,
   return lo;
 }
 
+// Merge-path splits of every chunk start of the merge pass at width w: the
+// number of pairs run a contributes to the outputs before the chunk (relative
+// to the chunk's pair of runs).  One thread per chunk, all in flight at once.
+__global__ void __launch_bounds__(kSortBlock)
+    sort_partition_kernel(const long long* __restrict__ long_lengths,
+                          const long long* __restrict__ long_base,
+                          const long long* __restrict__ cbase, long long nlong, long long w,
+                          const unsigned long long* __restrict__ skey,
+                          const long long* __restrict__ sidx, long long* __restrict__ splits) {
+  for (long long k = blockIdx.y; k < nlong; k += gridDim.y) {
+    const long long L = long_lengths[k], base = long_base[k];
+    if (L <= w) continue;
+    const long long nchunks = (L + kSortTile - 1) / kSortTile;
+    for (long long c = blockIdx.x * (long long)kSortBlock + threadIdx.x; c < nchunks;
+         c += (long long)gridDim.x * kSortBlock) {
+      const long long o0 = c * kSortTile;
+      const long long lo = o0 / (2 * w) * (2 * w);
+      const long long mid = lo + w < L ? lo + w : L, hi = lo + 2 * w < L ? lo + 2 * w : L;
+      splits[cbase[k] + c] = merge_split_g(skey + base + lo, sidx + base + lo, mid - lo,
+                                           skey + base + mid, sidx + base + mid, hi - mid, o0 - lo);
+    }
+  }
+}
+
+__global__ void long_chunks_kernel(const long long* __restrict__ lens, long long nlong,
+                                   long long* __restrict__ chunks) {
+  for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < nlong;
+       k += (long long)gridDim.x * blockDim.x)
+    chunks[k] = (lens[k] + kSortTile - 1) / kSortTile;
+}
+
 // One merge pass at run width w: runs [lo, lo+w) and [lo+w, lo+2w) of each
 // segment longer than w merge into 2w.  A CTA produces kSortTile consecutive
 // outputs of one pair (pairs are multiples of kSortTile long).
 __global__ void __launch_bounds__(kSortBlock)
     sort_merge_kernel(const long long* __restrict__ long_lengths,
-                      const long long* __restrict__ long_base, long long nlong, long long w,
+                      const long long* __restrict__ long_base, const long long* __restrict__ cbase,
+                      long long nlong, long long w, const long long* __restrict__ splits,
                       const unsigned long long* __restrict__ skey, const long long* __restrict__ sidx,
                       unsigned long long* __restrict__ dkey, long long* __restrict__ didx) {
   __shared__ unsigned long long s_key[kPadTile];
   __shared__ long long s_idx[kPadTile];
-  __shared__ long long s_a0, s_a1;
   for (long long k = blockIdx.y; k < nlong; k += gridDim.y) {
     const long long L = long_lengths[k], base = long_base[k];
     if (L <= w) continue;  // already one run: its pairs stay where its last pass put them
@@ -430,10 +462,11 @@ __global__ void __launch_bounds__(kSortBlock)
       const long long* ai = sidx + base + lo;
       const unsigned long long* bk = skey + base + mid;
       const long long* bi = sidx + base + mid;
-      if (threadIdx.x == 0) s_a0 = merge_split_g(ak, ai, na, bk, bi, nb, o0 - lo);
-      if (threadIdx.x == 32) s_a1 = merge_split_g(ak, ai, na, bk, bi, nb, o1 - lo);
-      __syncthreads();
-      const long long a0 = s_a0, a1 = s_a1;
+      // the chunk's bounding splits, found by the partition kernel (the next
+      // chunk's start when it lies in the same pair of runs)
+      const long long ci = cbase[k] + o0 / kSortTile;
+      const long long a0 = splits[ci];
+      const long long a1 = o1 == hi ? na : splits[ci + 1];
       const long long b0 = (o0 - lo) - a0, b1 = (o1 - lo) - a1;
       const int ca = (int)(a1 - a0), cb = (int)(b1 - b0);
       // stage this chunk's inputs: ca from run a, then cb from run b
@@ -506,7 +539,8 @@ __global__ void long_lengths_kernel(const U* __restrict__ offsets, long long len
 
 template <class T, class U, bool ARG>
 cudaError_t launch_sort(void* toptr, const T* fromptr, long long length, const U* offsets,
-                        long long offsetslength, bool ascending, cudaStream_t s) {
+                        long long offsetslength, bool ascending, uint64_t inv, uint64_t* err,
+                        cudaStream_t s) {
   if (length <= 0) return cudaSuccess;
   const long long nseg = offsetslength - 1;
   long long limit = length;
@@ -565,25 +599,40 @@ cudaError_t launch_sort(void* toptr, const T* fromptr, long long length, const U
     const long long maxl = (long long)hc[kCntLongMax];
     if (e == cudaSuccess && nlong > 0) {
       void* bufs = nullptr;
-      e = scratch_alloc(&bufs, 32 * (size_t)total, s);
+      // pair buffers A and B, then per long segment its chunk count and first
+      // chunk, then one split per chunk
+      const long long nsplit = total / kSortTile + nlong + 1;
+      e = scratch_alloc(&bufs, 32 * (size_t)total + 8 * (size_t)(2 * nlong + nsplit), s);
       if (e == cudaSuccess) {
         unsigned long long* akey = static_cast<unsigned long long*>(bufs);
         long long* aidx = reinterpret_cast<long long*>(akey + total);
         unsigned long long* bkey = reinterpret_cast<unsigned long long*>(aidx + total);
         long long* bidx = reinterpret_cast<long long*>(bkey + total);
+        long long* chunks_n = bidx + total;
+        long long* cbase = chunks_n + nlong;
+        long long* splits = cbase + nlong;
         const unsigned gy = (unsigned)(nlong < 65535 ? nlong : 65535);
         const long long chunks = (maxl + kSortTile - 1) / kSortTile;
         const unsigned gx = (unsigned)(chunks < 65535 ? chunks : 65535);
+        const long long pchunks = (chunks + kSortBlock - 1) / kSortBlock;
+        const unsigned pgx = (unsigned)(pchunks < 65535 ? pchunks : 65535);
         long_lengths_kernel<U><<<grid((nlong + 255) / 256), 256, 0, s>>>(offsets, length, long_ids,
                                                                         nlong, long_len);
-        sort_runs_kernel<T, U><<<dim3(gx, gy), kSortBlock, 0, s>>>(
-            fromptr, length, offsets, long_ids, long_base, nlong, ascending, akey, aidx);
+        long_chunks_kernel<<<grid((nlong + 255) / 256), 256, 0, s>>>(long_len, nlong, chunks_n);
         e = cudaGetLastError();
+        if (e == cudaSuccess) e = exclusive_scan_i64(chunks_n, cbase, nlong, nullptr, inv, err, s);
+        if (e == cudaSuccess) {
+          sort_runs_kernel<T, U><<<dim3(gx, gy), kSortBlock, 0, s>>>(
+              fromptr, length, offsets, long_ids, long_base, nlong, ascending, akey, aidx);
+          e = cudaGetLastError();
+        }
         int pass = 0;
         for (long long w = kSortTile; w < maxl && e == cudaSuccess; w <<= 1, pass++) {
           const bool even = (pass & 1) == 0;
+          sort_partition_kernel<<<dim3(pgx, gy), kSortBlock, 0, s>>>(
+              long_len, long_base, cbase, nlong, w, even ? akey : bkey, even ? aidx : bidx, splits);
           sort_merge_kernel<<<dim3(gx, gy), kSortBlock, 0, s>>>(
-              long_len, long_base, nlong, w, even ? akey : bkey, even ? aidx : bidx,
+              long_len, long_base, cbase, nlong, w, splits, even ? akey : bkey, even ? aidx : bidx,
               even ? bkey : akey, even ? bidx : aidx);
           e = cudaGetLastError();
         }
@@ -612,10 +661,9 @@ cudaError_t launch_sort(void* toptr, const T* fromptr, long long length, const U
                                                uint64_t invocation_index, uint64_t* err_code, \
                                                void* stream) {                                \
     (void)stable;                                                                             \
-    (void)invocation_index;                                                                   \
-    (void)err_code;                                                                           \
     return (int)launch_sort<T, U, true>(toptr, fromptr, length, offsets, offsetslength,        \
-                                        ascending, (cudaStream_t)stream);                     \
+                                        ascending, invocation_index, err_code,                \
+                                        (cudaStream_t)stream);                                \
   }
 #define GB_ARGSORT_ALL(SUF, T)                                                                 \
   GB_ARGSORT(SUF, T, int32, int32_t)                                                           \
@@ -628,8 +676,7 @@ cudaError_t launch_sort(void* toptr, const T* fromptr, long long length, const U
                                    bool ascending, bool stable, uint64_t invocation_index,    \
                                    uint64_t* err_code, void* stream) {                        \
     (void)stable;                                                                             \
-    (void)invocation_index;                                                                   \
-    (void)err_code;                                                                           \
     return (int)launch_sort<T, int64_t, false>(toptr, fromptr, length, offsets, offsetslength, \
-                                               ascending, (cudaStream_t)stream);              \
+                                               ascending, invocation_index, err_code,         \
+                                               (cudaStream_t)stream);                         \
   }
