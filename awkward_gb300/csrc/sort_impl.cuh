@@ -12,8 +12,8 @@
 // (key, index) are sorted ascending -- the index breaks ties, so the result
 // is the stable order (std::stable_sort's; it is also a valid answer when
 // `stable` is false).  Segments by length:
-//   <= 16        one thread: a bitonic network over registers (4, 8 or 16
-//                inputs, the size chosen per warp);
+//   <= 16        a tile of 256 segments: keys staged in shared memory, each
+//                element's rank (= output position) counted by one thread;
 //   <= 256       one warp: bitonic network in the warp's shared memory;
 //   <= 2048      one CTA: merge sort in shared memory (8 pairs per thread
 //                sorted in registers, then merge-path rounds);
@@ -42,7 +42,7 @@ using namespace gb;
 namespace {
 
 constexpr int kSortBlock = 256;
-constexpr int kThreadMax = 16;    // longest segment sorted by one thread
+constexpr int kThreadMax = 16;    // longest segment sorted by ranking its elements
 constexpr int kWarpMax = 256;     // ... by one warp
 constexpr int kSortTile = 2048;   // ... by one CTA; the run length of long segments
 constexpr int kMergePer = kSortTile / kSortBlock;  // outputs merged per thread
@@ -147,23 +147,17 @@ __device__ __forceinline__ void reg_bitonic(unsigned long long (&k)[N], I (&ix)[
   }
 }
 
-template <class T, bool ARG, int N>
-__device__ __forceinline__ void thread_sort(void* out, const T* x, long long st, int L, bool asc,
-                                            long long limit) {
-  unsigned long long k[N];
-  int ix[N];
-#pragma unroll
-  for (int j = 0; j < N; j++) {
-    k[j] = j < L ? sort_key(x[st + j], asc) : kPadKey;
-    ix[j] = j;  // pads carry the largest indices: they sort after real maxima
-  }
-  reg_bitonic<N, int>(k, ix);
-#pragma unroll
-  for (int j = 0; j < N; j++)
-    if (j < L) emit<T, ARG>(out, x, st, j, ix[j], limit);
-}
 
-// Sort the segments of <= 16 elements; list the others by class.
+// Sort the segments of <= 16 elements; list the others by class.  A CTA
+// takes 256 consecutive segments: the order keys of the short ones are staged
+// in shared memory (coalesced loads), then every element counts the keys of
+// its segment that precede it (smaller key, or equal key at a lower position)
+// -- its rank is its output position.  One thread per element: the work of a
+// segment is spread over its elements and no lane runs a network sized for
+// the longest segment of its warp.
+constexpr int kRankSegs = kSortBlock;              // segments per tile
+constexpr int kRankElems = kRankSegs * kThreadMax;  // staged keys per tile
+
 template <class T, class U, bool ARG>
 __global__ void __launch_bounds__(kSortBlock)
     sort_small_kernel(void* out, const T* __restrict__ x, long long length,
@@ -171,28 +165,27 @@ __global__ void __launch_bounds__(kSortBlock)
                       long long* __restrict__ lists, unsigned long long* counters,
                       long long* __restrict__ long_ids, long long* __restrict__ long_base,
                       long long long_cap) {
+  __shared__ unsigned long long s_key[kRankElems];
+  __shared__ unsigned char s_seg[kRankElems];  // tile segment of each staged key
+  __shared__ int s_loc[kRankSegs + 1];
+  __shared__ long long s_st[kRankSegs];
+  __shared__ int s_scan[kSortBlock / 32 + 1];
   const int lane = threadIdx.x & 31;
-  const long long warp0 = (blockIdx.x * (long long)kSortBlock + threadIdx.x) >> 5;
-  const long long nwarps = ((long long)gridDim.x * kSortBlock) >> 5;
-  for (long long base = warp0 * 32; base < nseg; base += nwarps * 32) {
-    const long long s = base + lane;
+  const long long ntiles = (nseg + kRankSegs - 1) / kRankSegs;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long long s = tile * kRankSegs + threadIdx.x;
     long long st = 0, sp = 0;
     if (s < nseg) seg_bounds(offsets, s, length, &st, &sp);
     const long long L = sp - st;
     const int cls = L <= 0 ? -1 : L <= kThreadMax ? 0 : L <= kWarpMax ? 1 : L <= kSortTile ? 2 : 3;
-    const unsigned need = __reduce_max_sync(0xffffffffu, cls == 0 ? (unsigned)L : 0u);
-    if (cls == 0) {
-      if (need <= 4) thread_sort<T, ARG, 4>(out, x, st, (int)L, asc, limit);
-      else if (need <= 8) thread_sort<T, ARG, 8>(out, x, st, (int)L, asc, limit);
-      else thread_sort<T, ARG, 16>(out, x, st, (int)L, asc, limit);
-    }
     // class lists: warps from the front of `lists`, CTAs from the back
 #pragma unroll
     for (int c = 1; c <= 2; c++) {
       const unsigned m = __ballot_sync(0xffffffffu, cls == c);
       if (m == 0) continue;
       unsigned long long b0 = 0;
-      if (lane == __ffs(m) - 1) b0 = atomicAdd(counters + (c == 1 ? kCntWarp : kCntCta), (unsigned long long)__popc(m));
+      if (lane == __ffs(m) - 1)
+        b0 = atomicAdd(counters + (c == 1 ? kCntWarp : kCntCta), (unsigned long long)__popc(m));
       b0 = __shfl_sync(0xffffffffu, b0, __ffs(m) - 1);
       if (cls == c) {
         const long long r = (long long)b0 + __popc(m & ((1u << lane) - 1u));
@@ -201,11 +194,39 @@ __global__ void __launch_bounds__(kSortBlock)
     }
     if (cls == 3) {
       const unsigned long long k = atomicAdd(counters + kCntLong, 1ull);
-      if ((long long)k >= long_cap) continue;  // only overlapping segments get here
-      long_ids[k] = s;
-      long_base[k] = (long long)atomicAdd(counters + kCntLongTotal, (unsigned long long)L);
-      atomicMax(counters + kCntLongMax, (unsigned long long)L);
+      if ((long long)k < long_cap) {  // beyond it only with overlapping segments
+        long_ids[k] = s;
+        long_base[k] = (long long)atomicAdd(counters + kCntLongTotal, (unsigned long long)L);
+        atomicMax(counters + kCntLongMax, (unsigned long long)L);
+      }
     }
+    // the short segments' local offsets
+    int total;
+    auto add = [](int a, int b) { return a + b; };
+    const int loc = block_exclusive_scan<kSortBlock>(cls == 0 ? (int)L : 0, add, 0, s_scan, &total);
+    s_loc[threadIdx.x] = loc;
+    s_st[threadIdx.x] = st;
+    if (threadIdx.x == 0) s_loc[kRankSegs] = total;
+    if (cls == 0)
+      for (int p = 0; p < (int)L; p++) s_seg[loc + p] = (unsigned char)threadIdx.x;
+    __syncthreads();
+    for (int q = threadIdx.x; q < total; q += kSortBlock) {
+      const int r = s_seg[q];
+      s_key[q] = sort_key(x[s_st[r] + (q - s_loc[r])], asc);
+    }
+    __syncthreads();
+    for (int q = threadIdx.x; q < total; q += kSortBlock) {
+      const int r = s_seg[q];
+      const int b = s_loc[r], n = s_loc[r + 1] - b, p = q - b;
+      const unsigned long long k = s_key[q];
+      int rank = 0;
+      for (int j = 0; j < n; j++) {
+        const unsigned long long kj = s_key[b + j];
+        rank += (kj < k) | ((kj == k) & (j < p));
+      }
+      emit<T, ARG>(out, x, s_st[r], rank, p, limit);
+    }
+    __syncthreads();
   }
 }
 
