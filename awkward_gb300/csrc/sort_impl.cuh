@@ -98,12 +98,25 @@ __device__ __forceinline__ void emit(void* out, const T* x, long long st, long l
   else if (st + j < limit) static_cast<T*>(out)[st + j] = x[st + local];
 }
 
+// The CPU's sort copies min(offsets[last], length) values (argsort: all of
+// them); every kernel reads it from the offsets itself, so the host needs no
+// copy of it.
+template <class U, bool ARG>
+__device__ __forceinline__ long long sort_limit(const U* offsets, long long olen,
+                                                long long length) {
+  if (ARG) return length;
+  if (olen <= 0) return 0;
+  const long long last = (long long)offsets[olen - 1];
+  return last < length ? last : length;
+}
+
 // Positions outside [offsets[0], offsets[last]): argsort keeps the iota, sort
 // copies through (below `limit`).
 template <class T, class U, bool ARG>
 __global__ void __launch_bounds__(kSortBlock)
     sort_gaps_kernel(void* out, const T* __restrict__ x, long long length, const U* offsets,
-                     long long nseg, long long limit) {
+                     long long nseg) {
+  const long long limit = sort_limit<U, ARG>(offsets, nseg + 1, length);
   long long first = 0, last = 0;
   if (nseg >= 0) {
     first = (long long)offsets[0];
@@ -161,10 +174,11 @@ constexpr int kRankElems = kRankSegs * kThreadMax;  // staged keys per tile
 template <class T, class U, bool ARG>
 __global__ void __launch_bounds__(kSortBlock)
     sort_small_kernel(void* out, const T* __restrict__ x, long long length,
-                      const U* __restrict__ offsets, long long nseg, long long limit, bool asc,
+                      const U* __restrict__ offsets, long long nseg, bool asc,
                       long long* __restrict__ lists, unsigned long long* counters,
                       long long* __restrict__ long_ids, long long* __restrict__ long_base,
                       long long long_cap) {
+  const long long limit = sort_limit<U, ARG>(offsets, nseg + 1, length);
   __shared__ unsigned long long s_key[kRankElems];
   __shared__ unsigned char s_seg[kRankElems];  // tile segment of each staged key
   __shared__ int s_loc[kRankSegs + 1];
@@ -234,8 +248,9 @@ __global__ void __launch_bounds__(kSortBlock)
 template <class T, class U, bool ARG>
 __global__ void __launch_bounds__(kSortBlock)
     sort_warp_kernel(void* out, const T* __restrict__ x, long long length,
-                     const U* __restrict__ offsets, long long limit, bool asc,
+                     const U* __restrict__ offsets, long long nseg, bool asc,
                      const long long* __restrict__ lists, const unsigned long long* counters) {
+  const long long limit = sort_limit<U, ARG>(offsets, nseg + 1, length);
   __shared__ unsigned long long s_key[kSortBlock / 32][kWarpMax];
   __shared__ int s_idx[kSortBlock / 32][kWarpMax];
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -360,8 +375,9 @@ __device__ __forceinline__ void block_merge_sort(unsigned long long* s_key, I* s
 template <class T, class U, bool ARG>
 __global__ void __launch_bounds__(kSortBlock)
     sort_cta_kernel(void* out, const T* __restrict__ x, long long length,
-                    const U* __restrict__ offsets, long long nseg, long long limit, bool asc,
+                    const U* __restrict__ offsets, long long nseg, bool asc,
                     const long long* __restrict__ lists, const unsigned long long* counters) {
+  const long long limit = sort_limit<U, ARG>(offsets, nseg + 1, length);
   __shared__ unsigned long long s_key[kPadTile];
   __shared__ int s_idx[kPadTile];
   const long long n = (long long)counters[kCntCta];
@@ -532,7 +548,8 @@ __global__ void __launch_bounds__(kSortBlock)
                           const U* __restrict__ offsets, const long long* __restrict__ long_ids,
                           const long long* __restrict__ long_base, long long nlong,
                           const long long* __restrict__ aidx, const long long* __restrict__ bidx,
-                          long long limit) {
+                          long long nseg) {
+  const long long limit = sort_limit<U, ARG>(offsets, nseg + 1, length);
   for (long long k = blockIdx.y; k < nlong; k += gridDim.y) {
     long long st, sp;
     seg_bounds(offsets, long_ids[k], length, &st, &sp);
@@ -564,23 +581,10 @@ cudaError_t launch_sort(void* toptr, const T* fromptr, long long length, const U
                         cudaStream_t s) {
   if (length <= 0) return cudaSuccess;
   const long long nseg = offsetslength - 1;
-  long long limit = length;
-  if (!ARG) {
-    // the CPU gathers min(offsets[last], length) values; read offsets[last]
-    limit = 0;
-    if (offsetslength > 0) {
-      U last = 0;
-      cudaError_t e = cudaMemcpyAsync(&last, offsets + (offsetslength - 1), sizeof(U),
-                                      cudaMemcpyDeviceToHost, s);
-      if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-      if (e != cudaSuccess) return e;
-      limit = (long long)last < length ? (long long)last : length;
-    }
-  }
   const long long cap = (long long)device_sm_count() * 16;
   auto grid = [cap](long long want) { return (unsigned)(want < 1 ? 1 : want < cap ? want : cap); };
   sort_gaps_kernel<T, U, ARG><<<grid((length + kSortBlock - 1) / kSortBlock), kSortBlock, 0, s>>>(
-      toptr, fromptr, length, offsets, nseg < 0 ? -1 : nseg, limit);
+      toptr, fromptr, length, offsets, nseg < 0 ? -1 : nseg);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || nseg <= 0) return e;
   // class lists and counters
@@ -597,18 +601,18 @@ cudaError_t launch_sort(void* toptr, const T* fromptr, long long length, const U
   e = cudaMemsetAsync(counters, 0, sizeof(unsigned long long) * kCntWords, s);
   if (e == cudaSuccess) {
     sort_small_kernel<T, U, ARG><<<grid((nseg + kSortBlock - 1) / kSortBlock), kSortBlock, 0, s>>>(
-        toptr, fromptr, length, offsets, nseg, limit, ascending, lists, counters, long_ids,
+        toptr, fromptr, length, offsets, nseg, ascending, lists, counters, long_ids,
         long_base, long_cap);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
     sort_warp_kernel<T, U, ARG><<<(unsigned)cap, kSortBlock, 0, s>>>(
-        toptr, fromptr, length, offsets, limit, ascending, lists, counters);
+        toptr, fromptr, length, offsets, nseg, ascending, lists, counters);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
     sort_cta_kernel<T, U, ARG><<<(unsigned)cap, kSortBlock, 0, s>>>(
-        toptr, fromptr, length, offsets, nseg, limit, ascending, lists, counters);
+        toptr, fromptr, length, offsets, nseg, ascending, lists, counters);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess && length > kSortTile) {
@@ -661,7 +665,7 @@ cudaError_t launch_sort(void* toptr, const T* fromptr, long long length, const U
           const long long egx = (maxl + kSortBlock - 1) / kSortBlock;
           sort_long_emit_kernel<T, U, ARG>
               <<<dim3((unsigned)(egx < 65535 ? egx : 65535), gy), kSortBlock, 0, s>>>(
-                  toptr, fromptr, length, offsets, long_ids, long_base, nlong, aidx, bidx, limit);
+                  toptr, fromptr, length, offsets, long_ids, long_base, nlong, aidx, bidx, nseg);
           e = cudaGetLastError();
         }
         cudaError_t f = scratch_free(bufs, s);
