@@ -1072,7 +1072,7 @@ struct Error awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_fromshifts_
 }
 
 /* ======================================================================
- * Multi-core driver for the CPU baseline: run one reducer (any of the
+ * Multi-core runner for the CPU baseline: run one reducer (any of the
  * (toptr, fromptr, offsets, outlength) family above, or argmax/argmin with
  * `starts`) over `nthreads` contiguous list ranges.  Each thread calls the
  * single-threaded restatement on its own range; ranges never share an output.
