@@ -35,6 +35,10 @@ _FAMILY_MESSAGES = {
         "broadcast's offsets must be monotonically increasing",
         "cannot broadcast nested list",
     ],
+    # awkward_ListArray_compact_offsets.cu:15
+    "awkward_ListArray_compact_offsets": [
+        "stops[i] < starts[i]",
+    ],
     # awkward_ListArray_getitem_jagged_numvalid.cu:14-17
     "awkward_ListArray_getitem_jagged_numvalid": [
         "jagged slice's stops[i] < starts[i]",

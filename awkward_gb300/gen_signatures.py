@@ -86,6 +86,10 @@ FAMILIES = {
     "awkward_ByteMaskedArray_reduce_next_64": ("awkward_ByteMaskedArray_reduce_next_64.cpp", 7),
     "awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_64": ("awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_64.cpp", 7),
     "awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_fromshifts_64": ("awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_fromshifts_64.cpp", 7),
+    # list-layout conversions on the same path (ListArray -> offsets, regular carries)
+    "awkward_ListArray_compact_offsets": ("awkward_ListArray_compact_offsets.cpp", 7),
+    "awkward_RegularArray_getitem_carry": ("awkward_RegularArray_getitem_carry.cpp", 7),
+    "awkward_RegularArray_localindex": ("awkward_RegularArray_localindex.cpp", 7),
 }
 
 _C_TYPES = {

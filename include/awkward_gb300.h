@@ -95,6 +95,13 @@ int awkward_ListArray32_combinations_length_64(int64_t* totallen, int64_t* tooff
 int awkward_ListArray64_combinations_length_64(int64_t* totallen, int64_t* tooffsets, int64_t n, bool replacement, const int64_t* starts, const int64_t* stops, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* kernel-specification.yml:1195 */
 int awkward_ListArrayU32_combinations_length_64(int64_t* totallen, int64_t* tooffsets, int64_t n, bool replacement, const uint32_t* starts, const uint32_t* stops, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListArray_compact_offsets: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_compact_offsets.cpp:7 */
+/* kernel-specification.yml:1237 */
+int awkward_ListArray32_compact_offsets_64(int64_t* tooffsets, const int32_t* fromstarts, const int32_t* fromstops, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1243 */
+int awkward_ListArray64_compact_offsets_64(int64_t* tooffsets, const int64_t* fromstarts, const int64_t* fromstops, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1249 */
+int awkward_ListArrayU32_compact_offsets_64(int64_t* tooffsets, const uint32_t* fromstarts, const uint32_t* fromstops, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_ListArray_getitem_jagged_apply: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_getitem_jagged_apply.cpp:8 */
 /* kernel-specification.yml:1318 */
 int awkward_ListArray32_getitem_jagged_apply_64(int64_t* tooffsets, int64_t* tocarry, const int64_t* slicestarts, const int64_t* slicestops, int64_t sliceouterlen, const int64_t* sliceindex, int64_t sliceinnerlen, const int32_t* fromstarts, const int32_t* fromstops, int64_t contentlen, uint64_t invocation_index, uint64_t* err_code, void* stream);
@@ -177,12 +184,18 @@ int awkward_NumpyArray_reduce_mask_ByteMaskedArray_64(int8_t* toptr, const int64
 /* ---- awkward_RegularArray_combinations_64: replaces awkward-cpp/src/cpu-kernels/awkward_RegularArray_combinations_64.cpp:8 */
 /* kernel-specification.yml:2868 */
 int awkward_RegularArray_combinations_64(int64_t** tocarry, int64_t* toindex, int64_t* fromindex, int64_t n, bool replacement, int64_t size, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_RegularArray_getitem_carry: replaces awkward-cpp/src/cpu-kernels/awkward_RegularArray_getitem_carry.cpp:7 */
+/* kernel-specification.yml:2896 */
+int awkward_RegularArray_getitem_carry_64(int64_t* tocarry, const int64_t* fromcarry, int64_t lencarry, int64_t size, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_RegularArray_getitem_jagged_expand: replaces awkward-cpp/src/cpu-kernels/awkward_RegularArray_getitem_jagged_expand.cpp:8 */
 /* kernel-specification.yml:2912 */
 int awkward_RegularArray_getitem_jagged_expand_64(int64_t* multistarts, int64_t* multistops, const int64_t* singleoffsets, int64_t regularsize, int64_t regularlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_RegularArray_getitem_next_range: replaces awkward-cpp/src/cpu-kernels/awkward_RegularArray_getitem_next_range.cpp:8 */
 /* kernel-specification.yml:3014 */
 int awkward_RegularArray_getitem_next_range_64(int64_t* tocarry, int64_t regular_start, int64_t step, int64_t length, int64_t size, int64_t nextsize, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_RegularArray_localindex: replaces awkward-cpp/src/cpu-kernels/awkward_RegularArray_localindex.cpp:7 */
+/* kernel-specification.yml:3052 */
+int awkward_RegularArray_localindex_64(int64_t* toindex, int64_t size, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_RegularArray_reduce_local_nextparents_64: replaces awkward-cpp/src/cpu-kernels/awkward_RegularArray_reduce_local_nextparents_64.cpp:14 */
 /* kernel-specification.yml:3067 */
 int awkward_RegularArray_reduce_local_nextparents_64(int64_t* nextparents, int64_t size, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);

@@ -1072,6 +1072,41 @@ struct Error awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_fromshifts_
 }
 
 /* ======================================================================
+ * List-layout conversions (ListArray -> offsets, regular carries)
+ * ====================================================================== */
+
+/* awkward_ListArray_compact_offsets.cpp:7-23 */
+#define ORACLE_COMPACT_OFFSETS(NAME, C)                                        \
+  struct Error NAME(int64_t* tooffsets, const C* fromstarts, const C* fromstops, \
+                    int64_t length) {                                          \
+    tooffsets[0] = 0;                                                          \
+    for (int64_t i = 0; i < length; i++) {                                     \
+      if (fromstops[i] < fromstarts[i])                                        \
+        return failure("stops[i] < starts[i]", i, kSliceNone);                 \
+      tooffsets[i + 1] = tooffsets[i] + (int64_t)(fromstops[i] - fromstarts[i]); \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_COMPACT_OFFSETS(awkward_ListArray32_compact_offsets_64, int32_t)
+ORACLE_COMPACT_OFFSETS(awkward_ListArrayU32_compact_offsets_64, uint32_t)
+ORACLE_COMPACT_OFFSETS(awkward_ListArray64_compact_offsets_64, int64_t)
+
+/* awkward_RegularArray_getitem_carry.cpp:7-19 */
+struct Error awkward_RegularArray_getitem_carry_64(int64_t* tocarry, const int64_t* fromcarry,
+                                                   int64_t lencarry, int64_t size) {
+  for (int64_t i = 0; i < lencarry; i++)
+    for (int64_t j = 0; j < size; j++) tocarry[i * size + j] = fromcarry[i] * size + j;
+  return success();
+}
+
+/* awkward_RegularArray_localindex.cpp:7-18 */
+struct Error awkward_RegularArray_localindex_64(int64_t* toindex, int64_t size, int64_t length) {
+  for (int64_t i = 0; i < length; i++)
+    for (int64_t j = 0; j < size; j++) toindex[i * size + j] = j;
+  return success();
+}
+
+/* ======================================================================
  * Multi-core runner for the CPU baseline: run one reducer (any of the
  * (toptr, fromptr, offsets, outlength) family above, or argmax/argmin with
  * `starts`) over `nthreads` contiguous list ranges.  Each thread calls the

@@ -448,6 +448,43 @@ def nonlocal_cases(rng, name):
     return out
 
 
+def layout_cases(rng, name):
+    """Seeded inputs of compact_offsets and the RegularArray carries."""
+    rec = SIGNATURES[name]
+    fam = rec["family"]
+    args = {a[0]: a for a in rec["args"]}
+    S = 777
+    out = []
+    if fam == "awkward_ListArray_compact_offsets":
+        C = NP_DTYPES[args["fromstarts"][1]]
+        for n, bad in ((0, False), (1, False), (300, False), (120, True)):
+            L = _lengths(rng, n, 5, longs=(40,))
+            starts = rng.integers(0, 1000, n)
+            stops = starts + L
+            if bad and n:
+                stops[n // 2] = starts[n // 2] - 1 if starts[n // 2] > 0 else starts[n // 2]
+                if stops[n // 2] == starts[n // 2]:
+                    starts[n // 2] += 1
+            out.append({"tooffsets": np.full(n + 1, S, np.int64), "fromstarts": starts.astype(C),
+                        "fromstops": stops.astype(C), "length": n})
+    elif fam == "awkward_RegularArray_getitem_carry":
+        for lencarry, size in ((0, 3), (5, 0), (200, 4), (37, 1)):
+            out.append({"tocarry": np.full(lencarry * size, S, np.int64),
+                        "fromcarry": rng.integers(0, 500, lencarry).astype(np.int64),
+                        "lencarry": lencarry, "size": size})
+    elif fam == "awkward_RegularArray_localindex":
+        for size, length in ((0, 5), (3, 0), (5, 70), (1, 9)):
+            out.append({"toindex": np.full(size * length, S, np.int64), "size": size,
+                        "length": length})
+    else:
+        raise KeyError(fam)
+    return out
+
+
+LAYOUT_FAMILIES = ("awkward_ListArray_compact_offsets", "awkward_RegularArray_getitem_carry",
+                   "awkward_RegularArray_localindex")
+
+
 NONLOCAL_PREFIXES = ("awkward_ListOffsetArray_reduce_", "awkward_ListOffsetArray_local_",
                      "awkward_RegularArray_reduce_", "awkward_IndexedArray_",
                      "awkward_ByteMaskedArray_")
@@ -466,6 +503,8 @@ def make_random():
         rng = np.random.default_rng([20241203, zlib.crc32(name.encode())])
         if fam in ("awkward_argsort", "awkward_sort"):
             cases = sort_cases(rng, name)
+        elif fam in LAYOUT_FAMILIES:
+            cases = layout_cases(rng, name)
         elif fam.startswith(NONLOCAL_PREFIXES):
             cases = nonlocal_cases(rng, name)
         elif fam == "awkward_RegularArray_combinations_64":
