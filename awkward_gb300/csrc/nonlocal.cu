@@ -565,16 +565,18 @@ struct Regroup {
 };
 
 // Keys, values (and row positions) of the elements of the bins, sorted.
-cudaError_t regroup(Regroup& g, const long long* offsets, const long long* outer_offsets,
-                    long long outlength, long long maxcount, bool with_rib, uint64_t inv,
-                    uint64_t* err, cudaStream_t s) {
+cudaError_t regroup(Regroup& g, const long long* offsets, long long length,
+                    const long long* outer_offsets, long long outlength, long long maxcount,
+                    bool with_rib, uint64_t inv, uint64_t* err, cudaStream_t s) {
   {
     const long long* srcs[2] = {outer_offsets, outer_offsets + outlength};
     long long w[2];
     cudaError_t e = read_words(srcs, w, 2, s);
     if (e != cudaSuccess) return e;
-    g.R0 = w[0];
-    g.R1 = w[1] > w[0] ? w[1] : w[0];
+    // rows outside [0, length] have no offsets to read
+    const long long lim = length > 0 ? length : 0;
+    g.R0 = w[0] < 0 ? 0 : w[0] > lim ? lim : w[0];
+    g.R1 = w[1] < g.R0 ? g.R0 : w[1] > lim ? lim : w[1];
   }
   {
     const long long* srcs[2] = {offsets + g.R0, offsets + g.R1};
@@ -638,14 +640,13 @@ GB_EXPORT int awkward_ListOffsetArray_reduce_nonlocal_preparenext_64(
     int64_t length, const int64_t* outer_offsets, int64_t outlength, int64_t maxcount,
     uint64_t invocation_index, uint64_t* err_code, void* stream) {
   (void)offsetscopy;
-  (void)length;
   cudaStream_t s = (cudaStream_t)stream;
   const long long nb = (outlength > 0 && maxcount > 0) ? (long long)outlength * maxcount : 0;
   Regroup g;
   cudaError_t e = cudaSuccess;
   if (nb > 0)
-    e = regroup(g, (const long long*)offsets, (const long long*)outer_offsets, outlength, maxcount,
-                false, invocation_index, err_code, s);
+    e = regroup(g, (const long long*)offsets, length, (const long long*)outer_offsets, outlength,
+                maxcount, false, invocation_index, err_code, s);
   void* lbmem = nullptr;
   long long* lb = nullptr;
   if (e == cudaSuccess) e = scratch_alloc(&lbmem, sizeof(long long) * (size_t)(nb + 1), s);
@@ -709,7 +710,6 @@ GB_EXPORT int awkward_ListOffsetArray_reduce_nonlocal_nextshifts_64(
     int64_t length, const int64_t* starts, const int64_t* outer_offsets, int64_t outlength,
     int64_t maxcount, int64_t nextlen, const int64_t* nextcarry, uint64_t invocation_index,
     uint64_t* err_code, void* stream) {
-  (void)length;
   (void)starts;
   cudaStream_t s = (cudaStream_t)stream;
   if (outlength <= 0) return (int)cudaSuccess;  // nothing written, nothing to gather
@@ -719,8 +719,8 @@ GB_EXPORT int awkward_ListOffsetArray_reduce_nonlocal_nextshifts_64(
   cudaError_t e = cudaSuccess;
   void* lbmem = nullptr;
   if (nb > 0) {
-    e = regroup(g, (const long long*)offsets, (const long long*)outer_offsets, outlength, M, true,
-                invocation_index, err_code, s);
+    e = regroup(g, (const long long*)offsets, length, (const long long*)outer_offsets, outlength,
+                M, true, invocation_index, err_code, s);
     if (e == cudaSuccess && g.n > 0) {
       e = scratch_alloc(&lbmem, sizeof(long long) * (size_t)(nb + 1), s);
       if (e == cudaSuccess) e = fill_lower_bounds(g.skeys, g.n, (long long*)lbmem, nb + 1, s);
@@ -738,8 +738,10 @@ GB_EXPORT int awkward_ListOffsetArray_reduce_nonlocal_nextshifts_64(
     long long w[2];
     e = read_words(srcs, w, 2, s);
     if (e == cudaSuccess) {
-      const long long* srcs2[2] = {(const long long*)offsets + w[0],
-                                   (const long long*)offsets + (w[1] > w[0] ? w[1] : w[0])};
+      const long long lim = length > 0 ? length : 0;
+      const long long r0 = w[0] < 0 ? 0 : w[0] > lim ? lim : w[0];
+      const long long r1 = w[1] < r0 ? r0 : w[1] > lim ? lim : w[1];
+      const long long* srcs2[2] = {(const long long*)offsets + r0, (const long long*)offsets + r1};
       long long v[2];
       e = read_words(srcs2, v, 2, s);
       g.E0 = v[0];
