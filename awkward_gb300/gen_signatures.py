@@ -46,6 +46,15 @@ FAMILIES = {
     "awkward_reduce_sumofsquares": ("awkward_reduce_sumofsquares.cpp", 12),
     "awkward_reduce_sumofpowers": ("awkward_reduce_sumofpowers.cpp", 39),
     "awkward_reduce_centered_sumofsquares": ("awkward_reduce_centered_sumofsquares.cpp", 15),
+    "awkward_reduce_sum_complex": ("awkward_reduce_sum_complex.cpp", 7),
+    "awkward_reduce_prod_complex": ("awkward_reduce_prod_complex.cpp", 9),
+    "awkward_reduce_max_complex": ("awkward_reduce_max_complex.cpp", 7),
+    "awkward_reduce_min_complex": ("awkward_reduce_min_complex.cpp", 7),
+    "awkward_reduce_argmax_complex": ("awkward_reduce_argmax_complex.cpp", 7),
+    "awkward_reduce_argmin_complex": ("awkward_reduce_argmin_complex.cpp", 7),
+    "awkward_reduce_countnonzero_complex": ("awkward_reduce_countnonzero_complex.cpp", 7),
+    "awkward_reduce_sum_bool_complex": ("awkward_reduce_sum_bool_complex.cpp", 7),
+    "awkward_reduce_prod_bool_complex": ("awkward_reduce_prod_bool_complex.cpp", 7),
     "awkward_NumpyArray_reduce_adjust_starts_64": ("awkward_NumpyArray_reduce_adjust_starts_64.cpp", 7),
     "awkward_NumpyArray_reduce_mask_ByteMaskedArray_64": ("awkward_NumpyArray_reduce_mask_ByteMaskedArray_64.cpp", 7),
     # jagged getitem and the carries it feeds

@@ -312,6 +312,11 @@ int awkward_reduce_argmax_uint64_64(int64_t* toptr, const uint64_t* fromptr, con
 int awkward_reduce_argmax_float32_64(int64_t* toptr, const float* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* kernel-specification.yml:4290 */
 int awkward_reduce_argmax_float64_64(int64_t* toptr, const double* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_argmax_complex: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_argmax_complex.cpp:7 */
+/* kernel-specification.yml:4309 */
+int awkward_reduce_argmax_complex64_64(int64_t* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4315 */
+int awkward_reduce_argmax_complex128_64(int64_t* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_reduce_argmin: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_argmin.cpp:25 */
 /* kernel-specification.yml:4338 */
 int awkward_reduce_argmin_int8_64(int64_t* toptr, const int8_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
@@ -333,6 +338,11 @@ int awkward_reduce_argmin_uint64_64(int64_t* toptr, const uint64_t* fromptr, con
 int awkward_reduce_argmin_float32_64(int64_t* toptr, const float* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* kernel-specification.yml:4401 */
 int awkward_reduce_argmin_float64_64(int64_t* toptr, const double* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_argmin_complex: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_argmin_complex.cpp:7 */
+/* kernel-specification.yml:4420 */
+int awkward_reduce_argmin_complex64_64(int64_t* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4426 */
+int awkward_reduce_argmin_complex128_64(int64_t* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_reduce_count_64: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_count_64.cpp:7 */
 /* kernel-specification.yml:4449 */
 int awkward_reduce_count_64(int64_t* toptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
@@ -359,6 +369,11 @@ int awkward_reduce_countnonzero_uint64_64(int64_t* toptr, const uint64_t* frompt
 int awkward_reduce_countnonzero_float32_64(int64_t* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* kernel-specification.yml:4522 */
 int awkward_reduce_countnonzero_float64_64(int64_t* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_countnonzero_complex: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_countnonzero_complex.cpp:7 */
+/* kernel-specification.yml:4540 */
+int awkward_reduce_countnonzero_complex64_64(int64_t* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4546 */
+int awkward_reduce_countnonzero_complex128_64(int64_t* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_reduce_max: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_max.cpp:9 */
 /* kernel-specification.yml:4564 */
 int awkward_reduce_max_int8_int8_64(int8_t* toptr, const int8_t* fromptr, const int64_t* offsets, int64_t outlength, int8_t identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
@@ -380,6 +395,11 @@ int awkward_reduce_max_uint64_uint64_64(uint64_t* toptr, const uint64_t* fromptr
 int awkward_reduce_max_float32_float32_64(float* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, float identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* kernel-specification.yml:4627 */
 int awkward_reduce_max_float64_float64_64(double* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, double identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_max_complex: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_max_complex.cpp:7 */
+/* kernel-specification.yml:4647 */
+int awkward_reduce_max_complex64_complex64_64(float* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, float identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4654 */
+int awkward_reduce_max_complex128_complex128_64(double* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, double identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_reduce_min: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_min.cpp:26 */
 /* kernel-specification.yml:4680 */
 int awkward_reduce_min_int8_int8_64(int8_t* toptr, const int8_t* fromptr, const int64_t* offsets, int64_t outlength, int8_t identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
@@ -401,6 +421,11 @@ int awkward_reduce_min_uint64_uint64_64(uint64_t* toptr, const uint64_t* fromptr
 int awkward_reduce_min_float32_float32_64(float* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, float identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* kernel-specification.yml:4743 */
 int awkward_reduce_min_float64_float64_64(double* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, double identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_min_complex: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_min_complex.cpp:7 */
+/* kernel-specification.yml:4763 */
+int awkward_reduce_min_complex64_complex64_64(float* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, float identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4770 */
+int awkward_reduce_min_complex128_complex128_64(double* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, double identity, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_reduce_prod: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_prod.cpp:12 */
 /* kernel-specification.yml:4796 */
 int awkward_reduce_prod_int64_int8_64(int64_t* toptr, const int8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
@@ -434,6 +459,11 @@ int awkward_reduce_prod_uint32_uint16_64(uint32_t* toptr, const uint16_t* frompt
 int awkward_reduce_prod_int32_int32_64(int32_t* toptr, const int32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* kernel-specification.yml:4886 */
 int awkward_reduce_prod_uint32_uint32_64(uint32_t* toptr, const uint32_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_prod_complex: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_prod_complex.cpp:9 */
+/* kernel-specification.yml:4903 */
+int awkward_reduce_prod_complex64_complex64_64(float* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:4909 */
+int awkward_reduce_prod_complex128_complex128_64(double* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_reduce_prod_bool: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_prod_bool.cpp:10 */
 /* kernel-specification.yml:4933 */
 int awkward_reduce_prod_bool_bool_64(bool* toptr, const bool* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
@@ -457,6 +487,11 @@ int awkward_reduce_prod_bool_uint64_64(bool* toptr, const uint64_t* fromptr, con
 int awkward_reduce_prod_bool_float32_64(bool* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* kernel-specification.yml:4993 */
 int awkward_reduce_prod_bool_float64_64(bool* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_prod_bool_complex: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_prod_bool_complex.cpp:7 */
+/* kernel-specification.yml:5012 */
+int awkward_reduce_prod_bool_complex64_64(bool* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5018 */
+int awkward_reduce_prod_bool_complex128_64(bool* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_reduce_sum: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_sum.cpp:12 */
 /* kernel-specification.yml:5037 */
 int awkward_reduce_sum_int64_int8_64(int64_t* toptr, const int8_t* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
@@ -577,6 +612,11 @@ int awkward_reduce_centered_sumofsquares_float64_bool_64(double* toptr, const bo
 int awkward_reduce_centered_sumofsquares_float64_float32_64(double* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, const double* means, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* kernel-specification.yml:5433 */
 int awkward_reduce_centered_sumofsquares_float64_float64_64(double* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, const double* means, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_sum_complex: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_sum_complex.cpp:7 */
+/* kernel-specification.yml:5453 */
+int awkward_reduce_sum_complex64_complex64_64(float* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5459 */
+int awkward_reduce_sum_complex128_complex128_64(double* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_reduce_sum_bool: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_sum_bool.cpp:18 */
 /* kernel-specification.yml:5479 */
 int awkward_reduce_sum_bool_bool_64(bool* toptr, const bool* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
@@ -600,6 +640,11 @@ int awkward_reduce_sum_bool_uint64_64(bool* toptr, const uint64_t* fromptr, cons
 int awkward_reduce_sum_bool_float32_64(bool* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* kernel-specification.yml:5539 */
 int awkward_reduce_sum_bool_float64_64(bool* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_reduce_sum_bool_complex: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_sum_bool_complex.cpp:7 */
+/* kernel-specification.yml:5558 */
+int awkward_reduce_sum_bool_complex64_64(bool* toptr, const float* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:5564 */
+int awkward_reduce_sum_bool_complex128_64(bool* toptr, const double* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_reduce_sum_int32_bool_64: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_sum_int32_bool_64.cpp:7 */
 /* kernel-specification.yml:5583 */
 int awkward_reduce_sum_int32_bool_64(int32_t* toptr, const bool* fromptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);

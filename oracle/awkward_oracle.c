@@ -1072,6 +1072,119 @@ struct Error awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_fromshifts_
 }
 
 /* ======================================================================
+ * Complex reducers (interleaved re, im): awkward_reduce_*_complex.cpp
+ * ====================================================================== */
+
+/* awkward_reduce_sum_complex.cpp:7-24 */
+#define ORACLE_SUM_COMPLEX(NAME, T)                                            \
+  struct Error NAME(T* toptr, const T* fromptr, const int64_t* offsets,        \
+                    int64_t outlength) {                                       \
+    for (int64_t b = 0; b < outlength; b++) {                                  \
+      T re = 0, im = 0;                                                        \
+      for (int64_t i = offsets[b]; i < offsets[b + 1]; i++) {                  \
+        re += fromptr[2 * i];                                                  \
+        im += fromptr[2 * i + 1];                                              \
+      }                                                                        \
+      toptr[2 * b] = re;                                                       \
+      toptr[2 * b + 1] = im;                                                   \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_SUM_COMPLEX(awkward_reduce_sum_complex64_complex64_64, float)
+ORACLE_SUM_COMPLEX(awkward_reduce_sum_complex128_complex128_64, double)
+
+/* awkward_reduce_prod_complex.cpp:9-31 */
+#define ORACLE_PROD_COMPLEX(NAME, T)                                           \
+  struct Error NAME(T* toptr, const T* fromptr, const int64_t* offsets,        \
+                    int64_t outlength) {                                       \
+    for (int64_t b = 0; b < outlength; b++) {                                  \
+      T a = 1, bb = 0;                                                         \
+      for (int64_t i = offsets[b]; i < offsets[b + 1]; i++) {                  \
+        const T c = fromptr[2 * i], d = fromptr[2 * i + 1];                    \
+        const T na = a * c - bb * d, nb = a * d + bb * c;                      \
+        a = na;                                                                \
+        bb = nb;                                                               \
+      }                                                                        \
+      toptr[2 * b] = a;                                                        \
+      toptr[2 * b + 1] = bb;                                                   \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_PROD_COMPLEX(awkward_reduce_prod_complex64_complex64_64, float)
+ORACLE_PROD_COMPLEX(awkward_reduce_prod_complex128_complex128_64, double)
+
+/* awkward_reduce_max_complex.cpp:7-33 / awkward_reduce_min_complex.cpp:7-33:
+ * the first element seeds; a later one replaces the best when it is
+ * lexicographically greater (smaller) by (re, im). */
+#define ORACLE_EXT_COMPLEX(NAME, T, OP)                                        \
+  struct Error NAME(T* toptr, const T* fromptr, const int64_t* offsets,        \
+                    int64_t outlength, T identity) {                           \
+    for (int64_t b = 0; b < outlength; b++) {                                  \
+      T bre = identity, bim = 0;                                               \
+      int seen = 0;                                                            \
+      for (int64_t i = offsets[b]; i < offsets[b + 1]; i++) {                  \
+        const T x = fromptr[2 * i], y = fromptr[2 * i + 1];                    \
+        if (!seen || x OP bre || (x == bre && y OP bim)) {                     \
+          bre = x;                                                             \
+          bim = y;                                                             \
+          seen = 1;                                                            \
+        }                                                                      \
+      }                                                                        \
+      toptr[2 * b] = bre;                                                      \
+      toptr[2 * b + 1] = bim;                                                  \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_EXT_COMPLEX(awkward_reduce_max_complex64_complex64_64, float, >)
+ORACLE_EXT_COMPLEX(awkward_reduce_max_complex128_complex128_64, double, >)
+ORACLE_EXT_COMPLEX(awkward_reduce_min_complex64_complex64_64, float, <)
+ORACLE_EXT_COMPLEX(awkward_reduce_min_complex128_complex128_64, double, <)
+
+/* awkward_reduce_argmax_complex.cpp:7-33 / argmin: the global index of that element. */
+#define ORACLE_ARG_COMPLEX(NAME, T, OP)                                        \
+  struct Error NAME(int64_t* toptr, const T* fromptr, const int64_t* offsets,  \
+                    int64_t outlength) {                                       \
+    for (int64_t b = 0; b < outlength; b++) {                                  \
+      int64_t best = -1;                                                       \
+      for (int64_t i = offsets[b]; i < offsets[b + 1]; i++) {                  \
+        if (best == -1) {                                                      \
+          best = i;                                                            \
+        } else {                                                               \
+          const T x = fromptr[2 * i], y = fromptr[2 * i + 1];                  \
+          const T bx = fromptr[2 * best], by = fromptr[2 * best + 1];          \
+          if (x OP bx || (x == bx && y OP by)) best = i;                       \
+        }                                                                      \
+      }                                                                        \
+      toptr[b] = best;                                                         \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_ARG_COMPLEX(awkward_reduce_argmax_complex64_64, float, >)
+ORACLE_ARG_COMPLEX(awkward_reduce_argmax_complex128_64, double, >)
+ORACLE_ARG_COMPLEX(awkward_reduce_argmin_complex64_64, float, <)
+ORACLE_ARG_COMPLEX(awkward_reduce_argmin_complex128_64, double, <)
+
+/* awkward_reduce_countnonzero_complex.cpp:7-21, _sum_bool_complex (any element
+ * nonzero), _prod_bool_complex (every element nonzero). */
+#define ORACLE_NONZERO_COMPLEX(NAME, OUT, T, MODE)                             \
+  struct Error NAME(OUT* toptr, const T* fromptr, const int64_t* offsets,      \
+                    int64_t outlength) {                                       \
+    for (int64_t b = 0; b < outlength; b++) {                                  \
+      int64_t nz = 0, n = offsets[b + 1] - offsets[b];                         \
+      for (int64_t i = offsets[b]; i < offsets[b + 1]; i++)                    \
+        nz += (fromptr[2 * i] != 0 || fromptr[2 * i + 1] != 0);                \
+      toptr[b] = MODE == 0 ? (OUT)nz : MODE == 1 ? (OUT)(nz > 0) : (OUT)(nz == n || n <= 0); \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_NONZERO_COMPLEX(awkward_reduce_countnonzero_complex64_64, int64_t, float, 0)
+ORACLE_NONZERO_COMPLEX(awkward_reduce_countnonzero_complex128_64, int64_t, double, 0)
+ORACLE_NONZERO_COMPLEX(awkward_reduce_sum_bool_complex64_64, bool, float, 1)
+ORACLE_NONZERO_COMPLEX(awkward_reduce_sum_bool_complex128_64, bool, double, 1)
+ORACLE_NONZERO_COMPLEX(awkward_reduce_prod_bool_complex64_64, bool, float, 2)
+ORACLE_NONZERO_COMPLEX(awkward_reduce_prod_bool_complex128_64, bool, double, 2)
+
+/* ======================================================================
  * List-layout conversions (ListArray -> offsets, regular carries)
  * ====================================================================== */
 

@@ -4,7 +4,7 @@ Two libraries:
 
 * ``oracle/liboracle.so`` -- ``awkward_oracle.c``, the plain-C restatement of
   the awkward-cpp kernels on the accelerated path.  Built everywhere (here
-  and on the GPU host) with ``gcc -O2 -shared -fPIC``.
+  and on the GPU host) with ``gcc -O2 -ffp-contract=off -shared -fPIC``.
 * ``oracle/_ref/libawkward-cpu-kernels.so`` -- awkward-cpp's OWN CPU kernels
   for the same families, compiled directly from the reference sources where
   they lie (``<awkward>/awkward-cpp/src/cpu-kernels/*.cpp``), used only to pin
@@ -41,8 +41,9 @@ def _stale(target, sources):
 def build_oracle(force=False):
     src = os.path.join(HERE, "awkward_oracle.c")
     if force or _stale(ORACLE_SO, [src]):
-        cmd = ["gcc", "-O2", "-std=c11", "-shared", "-fPIC", "-pthread", src, "-o",
-               ORACLE_SO + ".tmp", "-lm"]
+        # no fused multiply-adds: the same roundings on x86 and Arm hosts
+        cmd = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-shared", "-fPIC", "-pthread", src,
+               "-o", ORACLE_SO + ".tmp", "-lm"]
         subprocess.check_call(cmd)
         os.replace(ORACLE_SO + ".tmp", ORACLE_SO)
     return ORACLE_SO

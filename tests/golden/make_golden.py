@@ -448,6 +448,39 @@ def nonlocal_cases(rng, name):
     return out
 
 
+def complex_cases(rng, name):
+    """Seeded inputs of the complex reducers: interleaved (re, im) values with
+    ties, signed zeros, infinities and NaN in either part (some lists start
+    with a NaN real part), lists up to 1025 elements."""
+    rec = SIGNATURES[name]
+    args = {a[0]: a for a in rec["args"]}
+    base = args["fromptr"][1]
+    dt = NP_DTYPES[base]
+    out = []
+    for lam, nan_rate in ((4, 0.0), (4, 0.08), (2, 0.3)):
+        L = _lengths(rng, 250, lam)
+        off = _offsets(L)
+        E = int(off[-1])
+        v = np.round(rng.standard_normal((E, 2)), 1).astype(dt)  # ties in both parts
+        k = rng.random((E, 2))
+        v[k < nan_rate] = np.nan
+        v[(k >= 0.5) & (k < 0.53)] = 0.0
+        v[(k >= 0.53) & (k < 0.55)] = -0.0
+        v[(k >= 0.55) & (k < 0.56)] = np.inf
+        v[(k >= 0.56) & (k < 0.57)] = -np.inf
+        if nan_rate:
+            first = off[:-1][(L > 0) & (rng.random(len(L)) < 0.1)]
+            v[first, 0] = np.nan
+        kw = {"fromptr": v.reshape(-1), "offsets": off, "outlength": len(L)}
+        out_t = args["toptr"][1]
+        width = 2 if out_t in ("float", "double") else 1
+        kw["toptr"] = np.full(width * len(L), 123, NP_DTYPES[out_t])
+        if "identity" in args:
+            kw["identity"] = float(-np.inf if "max" in name else np.inf)
+        out.append(kw)
+    return out
+
+
 def layout_cases(rng, name):
     """Seeded inputs of compact_offsets and the RegularArray carries."""
     rec = SIGNATURES[name]
@@ -503,6 +536,8 @@ def make_random():
         rng = np.random.default_rng([20241203, zlib.crc32(name.encode())])
         if fam in ("awkward_argsort", "awkward_sort"):
             cases = sort_cases(rng, name)
+        elif fam.startswith("awkward_reduce") and fam.endswith("_complex"):
+            cases = complex_cases(rng, name)
         elif fam in LAYOUT_FAMILIES:
             cases = layout_cases(rng, name)
         elif fam.startswith(NONLOCAL_PREFIXES):

@@ -158,6 +158,11 @@ def is_float_sum_like(name):
         "awkward_reduce_sumofpowers", "awkward_reduce_centered_sumofsquares")
 
 
+def is_complex_sum(name):
+    """The complex sums: two order-dependent float outputs per list."""
+    return SIGNATURES[name]["family"] == "awkward_reduce_sum_complex"
+
+
 def assert_outputs_equal(name, got, expected, exact=True):
     """Compare outputs; ``exact`` demands bit-for-bit equality (NaN == NaN)."""
     for an, exp in expected.items():

@@ -73,6 +73,41 @@ def check_float_sum_like(name, kw, got, exp):
     assert not bad.any(), (name, np.nonzero(bad)[0][:5], got[bad][:5], exp[bad][:5], bound[bad][:5])
 
 
+def check_complex_sum(name, kw, got, exp):
+    """Per list and component: within 4*n*eps*sum|part| of awkward-cpp's sum."""
+    from awkward_gb300._signatures import SIGNATURES
+
+    eps = np.finfo(np.float32 if SIGNATURES[name]["args"][0][1] == "float" else np.float64).eps
+    off = np.asarray(kw["offsets"])
+    n = np.diff(off).astype(np.float64)
+    x = np.asarray(kw["fromptr"]).astype(np.float64).reshape(-1, 2)
+    m = min(len(n), len(exp) // 2)  # unit cases may list fewer outputs than lists
+    got = np.asarray(got)[: 2 * m].astype(np.float64).reshape(-1, 2)
+    exp = np.asarray(exp)[: 2 * m].astype(np.float64).reshape(-1, 2)
+    n, off = n[:m], off[: m + 1]
+    for c in range(2):
+        g, e = got[:, c], exp[:, c]
+        np.testing.assert_array_equal(np.isnan(g), np.isnan(e))
+        np.testing.assert_array_equal(g[np.isinf(e)], e[np.isinf(e)])
+        t = np.abs(x[:, c])
+        t = np.where(np.isfinite(t), t, 0.0)
+        cs = np.concatenate([[0.0], np.cumsum(t)])
+        bound = 4 * np.maximum(n, 1) * eps * (cs[off[1:]] - cs[off[:-1]])
+        fin = np.isfinite(e)
+        with np.errstate(invalid="ignore"):
+            bad = fin & ~(np.abs(g - e) <= bound)
+        assert not bad.any(), (name, c, np.nonzero(bad)[0][:5])
+
+
+def check(name, kw, outs, expected):
+    if gc.is_complex_sum(name):
+        check_complex_sum(name, kw, outs["toptr"], expected["toptr"])
+    elif gc.is_float_sum_like(name):
+        check_float_sum_like(name, kw, outs["toptr"], expected["toptr"])
+    else:
+        gc.assert_outputs_equal(name, outs, expected, exact=True)
+
+
 @pytest.mark.parametrize("name,index", UNIT, ids=[f"{n}-{i}" for n, i in UNIT])
 def test_gpu_kernel_test_data(name, index):
     kw, expected, message = gc.unit_case(name, index)
@@ -81,10 +116,7 @@ def test_gpu_kernel_test_data(name, index):
         assert err is not None and err.startswith(message), (err, message)
         return
     assert err is None, err
-    if gc.is_float_sum_like(name):
-        check_float_sum_like(name, kw, outs["toptr"], expected["toptr"])
-    else:
-        gc.assert_outputs_equal(name, outs, expected, exact=True)
+    check(name, kw, outs, expected)
 
 
 @pytest.mark.parametrize("name,index", RANDOM, ids=[f"{n}-{i}" for n, i in RANDOM])
@@ -95,7 +127,4 @@ def test_gpu_matches_awkward_cpp(name, index):
         assert err is not None and err.startswith(error), (err, error)
         return
     assert err is None, err
-    if gc.is_float_sum_like(name):
-        check_float_sum_like(name, kw, outs["toptr"], expected["toptr"])
-    else:
-        gc.assert_outputs_equal(name, outs, expected, exact=True)
+    check(name, kw, outs, expected)
