@@ -106,6 +106,34 @@ __device__ __forceinline__ void tile_for_each_slot(const TileSmem& sm, long long
   }
 }
 
+// Stage the tile of lists [l0, l0 + kTileLists) (those below n): sm.loc holds
+// the local exclusive offsets of their (non-negative) counts; returns the
+// tile's total count.  All threads call it.
+template <class CountFn>
+__device__ __forceinline__ long long stage_lists(TileSmem& sm, long long l0, long long n,
+                                                 CountFn count) {
+  long long c[kTileLPT];
+  long long sum = 0;
+#pragma unroll
+  for (int r = 0; r < kTileLPT; r++) {
+    const long long l = l0 + threadIdx.x * kTileLPT + r;
+    c[r] = l < n ? count(l) : 0;
+    if (c[r] < 0) c[r] = 0;
+    sum += c[r];
+  }
+  long long total;
+  auto add = [](long long a, long long b) { return a + b; };
+  long long run = block_exclusive_scan<kTileBlock>(sum, add, 0ll, sm.scan, &total);
+#pragma unroll
+  for (int r = 0; r < kTileLPT; r++) {
+    sm.loc[threadIdx.x * kTileLPT + r] = run;
+    run += c[r];
+  }
+  if (threadIdx.x == 0) sm.loc[kTileLists] = total;
+  __syncthreads();
+  return total;
+}
+
 inline long long tile_count(long long n) { return (n + kTileLists - 1) / kTileLists; }
 
 }  // namespace gb

@@ -16,6 +16,8 @@
 //                     local_preparenext_64                      (.cpp:7-31)
 //   ByteMaskedArray   reduce_next_64                            (.cpp:7-32)
 //                     reduce_next_nonlocal_nextshifts[_fromshifts]_64
+//   Content           getitem_next_missing_jagged_getmaskstartstop (.cpp:7-28)
+//   MaskedArray       getitem_next_jagged_project (32/U32/64)   (.cpp:7-25)
 //
 // The non-local "preparenext" regroups the elements of every outer bin column
 // by column: next bin b*maxcount + col lists column `col` of each row of bin b
@@ -58,35 +60,6 @@ cudaError_t read_words(const long long* const* srcs, long long* dst, int n, cuda
     if (e != cudaSuccess) return e;
   }
   return cudaStreamSynchronize(s);
-}
-
-// ---------------------------------------------------------------- list tiles
-// Stage the tile of lists [l0, l0 + kTileLists) (those below n): sm.loc holds
-// the local exclusive offsets of their (non-negative) counts; returns the
-// tile's total count.  All threads call it.
-template <class CountFn>
-__device__ __forceinline__ long long stage_lists(TileSmem& sm, long long l0, long long n,
-                                                 CountFn count) {
-  long long c[kTileLPT];
-  long long sum = 0;
-#pragma unroll
-  for (int r = 0; r < kTileLPT; r++) {
-    const long long l = l0 + threadIdx.x * kTileLPT + r;
-    c[r] = l < n ? count(l) : 0;
-    if (c[r] < 0) c[r] = 0;
-    sum += c[r];
-  }
-  long long total;
-  auto add = [](long long a, long long b) { return a + b; };
-  long long run = block_exclusive_scan<kTileBlock>(sum, add, 0ll, sm.scan, &total);
-#pragma unroll
-  for (int r = 0; r < kTileLPT; r++) {
-    sm.loc[threadIdx.x * kTileLPT + r] = run;
-    run += c[r];
-  }
-  if (threadIdx.x == 0) sm.loc[kTileLists] = total;
-  __syncthreads();
-  return total;
 }
 
 // ------------------------------------------------ maxcount and offsets copy
@@ -364,7 +337,9 @@ constexpr int kCWarps = kBlock / 32;
 constexpr int kCWarpSpan = kCSteps * 32;        // 512 consecutive entries per warp
 constexpr int kCTile = kCWarps * kCWarpSpan;    // 4096 entries per tile
 
-enum CompactMode { kReduceNext = 0, kNextShifts = 1 };
+// kMaskStartStop: Content_getitem_next_missing_jagged_getmaskstartstop;
+// kProject: MaskedArray_getitem_next_jagged_project.
+enum CompactMode { kReduceNext = 0, kNextShifts = 1, kMaskStartStop = 2, kProject = 3 };
 
 template <class T, bool MASKED, int MODE, bool FROMSHIFTS>
 struct CompactArgs {
@@ -378,6 +353,12 @@ struct CompactArgs {
   long long* outindex;
   long long* nextshifts;
   const long long* shifts;
+  const long long* offsets_in;  // kMaskStartStop
+  long long* mask_out;
+  const long long* starts_in;   // kProject
+  const long long* stops_in;
+  long long* starts_out;        // kMaskStartStop, kProject
+  long long* stops_out;
   long long e0, e1;  // entries [e0, e1)
 };
 
@@ -444,8 +425,17 @@ __global__ void __launch_bounds__(kBlock)
         } else {
           a.outindex[e] = -1;
         }
-      } else {
+      } else if constexpr (MODE == kNextShifts) {
         if (v) a.nextshifts[k] = (FROMSHIFTS ? a.shifts[e] : 0ll) + (e - k);
+      } else if constexpr (MODE == kMaskStartStop) {
+        a.starts_out[e] = a.offsets_in[k];
+        a.mask_out[e] = v ? e : -1;
+        a.stops_out[e] = a.offsets_in[k + (v ? 1 : 0)];
+      } else {
+        if (v) {
+          a.starts_out[k] = a.starts_in[e];
+          a.stops_out[k] = a.stops_in[e];
+        }
       }
     }
     run += __popc(m[j]);
@@ -1000,3 +990,36 @@ GB_EXPORT int awkward_IndexedArray_local_preparenext_64(int64_t* tocarry, const 
       (long long*)tocarry, (const long long*)offsets, (const long long*)nextoffsets, outlength);
   return (int)cudaGetLastError();
 }
+
+GB_EXPORT int awkward_Content_getitem_next_missing_jagged_getmaskstartstop(
+    int64_t* index_in, int64_t* offsets_in, int64_t* mask_out, int64_t* starts_out,
+    int64_t* stops_out, int64_t length, uint64_t invocation_index, uint64_t* err_code,
+    void* stream) {
+  CompactArgs<int64_t, false, kMaskStartStop, false> a{};
+  a.index = index_in;
+  a.offsets_in = (const long long*)offsets_in;
+  a.mask_out = (long long*)mask_out;
+  a.starts_out = (long long*)starts_out;
+  a.stops_out = (long long*)stops_out;
+  a.e0 = 0;
+  a.e1 = length < 0 ? 0 : length;
+  return (int)launch_compact(a, invocation_index, err_code, (cudaStream_t)stream);
+}
+
+#define GB_JAGGED_PROJECT(NAME, T)                                                              \
+  GB_EXPORT int NAME(T* index, int64_t* starts_in, int64_t* stops_in, int64_t* starts_out,     \
+                     int64_t* stops_out, int64_t length, uint64_t invocation_index,             \
+                     uint64_t* err_code, void* stream) {                                        \
+    CompactArgs<T, false, kProject, false> a{};                                                 \
+    a.index = index;                                                                            \
+    a.starts_in = (const long long*)starts_in;                                                  \
+    a.stops_in = (const long long*)stops_in;                                                    \
+    a.starts_out = (long long*)starts_out;                                                      \
+    a.stops_out = (long long*)stops_out;                                                        \
+    a.e0 = 0;                                                                                   \
+    a.e1 = length < 0 ? 0 : length;                                                             \
+    return (int)launch_compact(a, invocation_index, err_code, (cudaStream_t)stream);            \
+  }
+GB_JAGGED_PROJECT(awkward_MaskedArray32_getitem_next_jagged_project, int32_t)
+GB_JAGGED_PROJECT(awkward_MaskedArrayU32_getitem_next_jagged_project, uint32_t)
+GB_JAGGED_PROJECT(awkward_MaskedArray64_getitem_next_jagged_project, int64_t)

@@ -99,6 +99,16 @@ FAMILIES = {
     "awkward_ListArray_compact_offsets": ("awkward_ListArray_compact_offsets.cpp", 7),
     "awkward_RegularArray_getitem_carry": ("awkward_RegularArray_getitem_carry.cpp", 7),
     "awkward_RegularArray_localindex": ("awkward_RegularArray_localindex.cpp", 7),
+    # small siblings on the same driver paths (argmax through option types,
+    # axis-0 local index, range slices with advanced indexing, jagged slices
+    # with missing values)
+    "awkward_NumpyArray_reduce_adjust_starts_shifts_64": ("awkward_NumpyArray_reduce_adjust_starts_shifts_64.cpp", 7),
+    "awkward_localindex": ("awkward_localindex.cpp", 8),
+    "awkward_ListArray_getitem_next_range_counts": ("awkward_ListArray_getitem_next_range_counts.cpp", 7),
+    "awkward_ListArray_getitem_next_range_spreadadvanced": ("awkward_ListArray_getitem_next_range_spreadadvanced.cpp", 7),
+    "awkward_RegularArray_getitem_next_range_spreadadvanced": ("awkward_RegularArray_getitem_next_range_spreadadvanced.cpp", 7),
+    "awkward_Content_getitem_next_missing_jagged_getmaskstartstop": ("awkward_Content_getitem_next_missing_jagged_getmaskstartstop.cpp", 7),
+    "awkward_MaskedArray_getitem_next_jagged_project": ("awkward_MaskedArray_getitem_next_jagged_project.cpp", 7),
 }
 
 _C_TYPES = {

@@ -47,6 +47,9 @@ int awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_64(int64_t* nextshif
 /* ---- awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_fromshifts_64: replaces awkward-cpp/src/cpu-kernels/awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_fromshifts_64.cpp:7 */
 /* kernel-specification.yml:284 */
 int awkward_ByteMaskedArray_reduce_next_nonlocal_nextshifts_fromshifts_64(int64_t* nextshifts, const int8_t* mask, int64_t length, bool valid_when, const int64_t* shifts, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_Content_getitem_next_missing_jagged_getmaskstartstop: replaces awkward-cpp/src/cpu-kernels/awkward_Content_getitem_next_missing_jagged_getmaskstartstop.cpp:7 */
+/* kernel-specification.yml:323 */
+int awkward_Content_getitem_next_missing_jagged_getmaskstartstop(int64_t* index_in, int64_t* offsets_in, int64_t* mask_out, int64_t* starts_out, int64_t* stops_out, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_IndexedArray_local_preparenext_64: replaces awkward-cpp/src/cpu-kernels/awkward_IndexedArray_local_preparenext_64.cpp:7 */
 /* kernel-specification.yml:549 */
 int awkward_IndexedArray_local_preparenext_64(int64_t* tocarry, const int64_t* starts, const int64_t* offsets, const int64_t* nextoffsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
@@ -146,6 +149,20 @@ int awkward_ListArray32_getitem_next_range_carrylength(int64_t* carrylength, con
 int awkward_ListArray64_getitem_next_range_carrylength(int64_t* carrylength, const int64_t* fromstarts, const int64_t* fromstops, int64_t lenstarts, int64_t start, int64_t stop, int64_t step, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* kernel-specification.yml:1824 */
 int awkward_ListArrayU32_getitem_next_range_carrylength(int64_t* carrylength, const uint32_t* fromstarts, const uint32_t* fromstops, int64_t lenstarts, int64_t start, int64_t stop, int64_t step, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListArray_getitem_next_range_counts: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_getitem_next_range_counts.cpp:7 */
+/* kernel-specification.yml:1865 */
+int awkward_ListArray32_getitem_next_range_counts_64(int64_t* total, const int32_t* fromoffsets, int64_t lenstarts, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1870 */
+int awkward_ListArray64_getitem_next_range_counts_64(int64_t* total, const int64_t* fromoffsets, int64_t lenstarts, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1875 */
+int awkward_ListArrayU32_getitem_next_range_counts_64(int64_t* total, const uint32_t* fromoffsets, int64_t lenstarts, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_ListArray_getitem_next_range_spreadadvanced: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_getitem_next_range_spreadadvanced.cpp:7 */
+/* kernel-specification.yml:1890 */
+int awkward_ListArray32_getitem_next_range_spreadadvanced_64(int64_t* toadvanced, const int64_t* fromadvanced, const int32_t* fromoffsets, int64_t lenstarts, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1896 */
+int awkward_ListArray64_getitem_next_range_spreadadvanced_64(int64_t* toadvanced, const int64_t* fromadvanced, const int64_t* fromoffsets, int64_t lenstarts, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:1902 */
+int awkward_ListArrayU32_getitem_next_range_spreadadvanced_64(int64_t* toadvanced, const int64_t* fromadvanced, const uint32_t* fromoffsets, int64_t lenstarts, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_ListArray_localindex: replaces awkward-cpp/src/cpu-kernels/awkward_ListArray_localindex.cpp:8 */
 /* kernel-specification.yml:1921 */
 int awkward_ListArray32_localindex_64(int64_t* toindex, const int32_t* offsets, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
@@ -175,9 +192,19 @@ int awkward_ListOffsetArray_reduce_nonlocal_outstartsstops_64(int64_t* outstarts
 /* ---- awkward_ListOffsetArray_reduce_nonlocal_preparenext_64: replaces awkward-cpp/src/cpu-kernels/awkward_ListOffsetArray_reduce_nonlocal_preparenext_64.cpp:7 */
 /* kernel-specification.yml:2298 */
 int awkward_ListOffsetArray_reduce_nonlocal_preparenext_64(int64_t* nextcarry, int64_t* nextoffsets, int64_t nextlen, int64_t* maxnextparents, int64_t* distincts, int64_t distinctslen, int64_t* offsetscopy, const int64_t* offsets, int64_t length, const int64_t* outer_offsets, int64_t outlength, int64_t maxcount, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_MaskedArray_getitem_next_jagged_project: replaces awkward-cpp/src/cpu-kernels/awkward_MaskedArray_getitem_next_jagged_project.cpp:7 */
+/* kernel-specification.yml:2486 */
+int awkward_MaskedArray32_getitem_next_jagged_project(int32_t* index, int64_t* starts_in, int64_t* stops_in, int64_t* starts_out, int64_t* stops_out, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:2494 */
+int awkward_MaskedArray64_getitem_next_jagged_project(int64_t* index, int64_t* starts_in, int64_t* stops_in, int64_t* starts_out, int64_t* stops_out, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* kernel-specification.yml:2502 */
+int awkward_MaskedArrayU32_getitem_next_jagged_project(uint32_t* index, int64_t* starts_in, int64_t* stops_in, int64_t* starts_out, int64_t* stops_out, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_NumpyArray_reduce_adjust_starts_64: replaces awkward-cpp/src/cpu-kernels/awkward_NumpyArray_reduce_adjust_starts_64.cpp:7 */
 /* kernel-specification.yml:2552 */
 int awkward_NumpyArray_reduce_adjust_starts_64(int64_t* toptr, int64_t outlength, const int64_t* offsets, const int64_t* starts, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_NumpyArray_reduce_adjust_starts_shifts_64: replaces awkward-cpp/src/cpu-kernels/awkward_NumpyArray_reduce_adjust_starts_shifts_64.cpp:7 */
+/* kernel-specification.yml:2568 */
+int awkward_NumpyArray_reduce_adjust_starts_shifts_64(int64_t* toptr, int64_t outlength, const int64_t* offsets, const int64_t* starts, const int64_t* shifts, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_NumpyArray_reduce_mask_ByteMaskedArray_64: replaces awkward-cpp/src/cpu-kernels/awkward_NumpyArray_reduce_mask_ByteMaskedArray_64.cpp:7 */
 /* kernel-specification.yml:2587 */
 int awkward_NumpyArray_reduce_mask_ByteMaskedArray_64(int8_t* toptr, const int64_t* offsets, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);
@@ -193,6 +220,9 @@ int awkward_RegularArray_getitem_jagged_expand_64(int64_t* multistarts, int64_t*
 /* ---- awkward_RegularArray_getitem_next_range: replaces awkward-cpp/src/cpu-kernels/awkward_RegularArray_getitem_next_range.cpp:8 */
 /* kernel-specification.yml:3014 */
 int awkward_RegularArray_getitem_next_range_64(int64_t* tocarry, int64_t regular_start, int64_t step, int64_t length, int64_t size, int64_t nextsize, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_RegularArray_getitem_next_range_spreadadvanced: replaces awkward-cpp/src/cpu-kernels/awkward_RegularArray_getitem_next_range_spreadadvanced.cpp:7 */
+/* kernel-specification.yml:3034 */
+int awkward_RegularArray_getitem_next_range_spreadadvanced_64(int64_t* toadvanced, const int64_t* fromadvanced, int64_t length, int64_t nextsize, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_RegularArray_localindex: replaces awkward-cpp/src/cpu-kernels/awkward_RegularArray_localindex.cpp:7 */
 /* kernel-specification.yml:3052 */
 int awkward_RegularArray_localindex_64(int64_t* toindex, int64_t size, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
@@ -291,6 +321,9 @@ int awkward_argsort_float64_uint32(int64_t* toptr, const double* fromptr, int64_
 int awkward_argsort_float64_uint64(int64_t* toptr, const double* fromptr, int64_t length, const uint64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* kernel-specification.yml:4111 */
 int awkward_argsort_float64_int64(int64_t* toptr, const double* fromptr, int64_t length, const int64_t* offsets, int64_t offsetslength, bool ascending, bool stable, uint64_t invocation_index, uint64_t* err_code, void* stream);
+/* ---- awkward_localindex: replaces awkward-cpp/src/cpu-kernels/awkward_localindex.cpp:8 */
+/* kernel-specification.yml:4196 */
+int awkward_localindex_64(int64_t* toindex, int64_t length, uint64_t invocation_index, uint64_t* err_code, void* stream);
 /* ---- awkward_reduce_argmax: replaces awkward-cpp/src/cpu-kernels/awkward_reduce_argmax.cpp:9 */
 /* kernel-specification.yml:4227 */
 int awkward_reduce_argmax_int8_64(int64_t* toptr, const int8_t* fromptr, const int64_t* offsets, const int64_t* starts, int64_t outlength, uint64_t invocation_index, uint64_t* err_code, void* stream);

@@ -1220,6 +1220,101 @@ struct Error awkward_RegularArray_localindex_64(int64_t* toindex, int64_t size, 
 }
 
 /* ======================================================================
+ * Small siblings on the same driver paths
+ * ====================================================================== */
+
+/* awkward_NumpyArray_reduce_adjust_starts_shifts_64.cpp:7-23 */
+struct Error awkward_NumpyArray_reduce_adjust_starts_shifts_64(int64_t* toptr, int64_t outlength,
+                                                               const int64_t* offsets,
+                                                               const int64_t* starts,
+                                                               const int64_t* shifts) {
+  (void)offsets;
+  for (int64_t k = 0; k < outlength; k++) {
+    const int64_t i = toptr[k];
+    if (i >= 0) toptr[k] += shifts[i] - starts[k];
+  }
+  return success();
+}
+
+/* awkward_localindex.cpp:8-14 */
+struct Error awkward_localindex_64(int64_t* toindex, int64_t length) {
+  for (int64_t i = 0; i < length; i++) toindex[i] = i;
+  return success();
+}
+
+/* awkward_ListArray_getitem_next_range_counts.cpp:7-18 */
+#define ORACLE_RANGE_COUNTS(NAME, C)                                           \
+  struct Error NAME(int64_t* total, const C* fromoffsets, int64_t lenstarts) { \
+    *total = 0;                                                                \
+    for (int64_t i = 0; i < lenstarts; i++)                                    \
+      *total = *total + fromoffsets[i + 1] - fromoffsets[i];                   \
+    return success();                                                          \
+  }
+ORACLE_RANGE_COUNTS(awkward_ListArray32_getitem_next_range_counts_64, int32_t)
+ORACLE_RANGE_COUNTS(awkward_ListArrayU32_getitem_next_range_counts_64, uint32_t)
+ORACLE_RANGE_COUNTS(awkward_ListArray64_getitem_next_range_counts_64, int64_t)
+
+/* awkward_ListArray_getitem_next_range_spreadadvanced.cpp:7-21 */
+#define ORACLE_RANGE_SPREAD(NAME, C)                                           \
+  struct Error NAME(int64_t* toadvanced, const int64_t* fromadvanced,          \
+                    const C* fromoffsets, int64_t lenstarts) {                 \
+    for (int64_t i = 0; i < lenstarts; i++) {                                  \
+      const C count = fromoffsets[i + 1] - fromoffsets[i];                     \
+      for (int64_t j = 0; j < (int64_t)count; j++)                             \
+        toadvanced[fromoffsets[i] + j] = fromadvanced[i];                      \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_RANGE_SPREAD(awkward_ListArray32_getitem_next_range_spreadadvanced_64, int32_t)
+ORACLE_RANGE_SPREAD(awkward_ListArrayU32_getitem_next_range_spreadadvanced_64, uint32_t)
+ORACLE_RANGE_SPREAD(awkward_ListArray64_getitem_next_range_spreadadvanced_64, int64_t)
+
+/* awkward_RegularArray_getitem_next_range_spreadadvanced.cpp:7-19 */
+struct Error awkward_RegularArray_getitem_next_range_spreadadvanced_64(int64_t* toadvanced,
+                                                                       const int64_t* fromadvanced,
+                                                                       int64_t length,
+                                                                       int64_t nextsize) {
+  for (int64_t i = 0; i < length; i++)
+    for (int64_t j = 0; j < nextsize; j++) toadvanced[i * nextsize + j] = fromadvanced[i];
+  return success();
+}
+
+/* awkward_Content_getitem_next_missing_jagged_getmaskstartstop.cpp:7-28 */
+struct Error awkward_Content_getitem_next_missing_jagged_getmaskstartstop(
+    int64_t* index_in, int64_t* offsets_in, int64_t* mask_out, int64_t* starts_out,
+    int64_t* stops_out, int64_t length) {
+  int64_t k = 0;
+  for (int64_t i = 0; i < length; i++) {
+    starts_out[i] = offsets_in[k];
+    if (index_in[i] < 0) {
+      mask_out[i] = -1;
+    } else {
+      mask_out[i] = i;
+      k++;
+    }
+    stops_out[i] = offsets_in[k];
+  }
+  return success();
+}
+
+/* awkward_MaskedArray_getitem_next_jagged_project.cpp:7-25 */
+#define ORACLE_JAGGED_PROJECT(NAME, T)                                         \
+  struct Error NAME(T* index, int64_t* starts_in, int64_t* stops_in,           \
+                    int64_t* starts_out, int64_t* stops_out, int64_t length) { \
+    int64_t k = 0;                                                             \
+    for (int64_t i = 0; i < length; i++)                                       \
+      if ((int64_t)index[i] >= 0) {                                            \
+        starts_out[k] = starts_in[i];                                          \
+        stops_out[k] = stops_in[i];                                            \
+        k++;                                                                   \
+      }                                                                        \
+    return success();                                                          \
+  }
+ORACLE_JAGGED_PROJECT(awkward_MaskedArray32_getitem_next_jagged_project, int32_t)
+ORACLE_JAGGED_PROJECT(awkward_MaskedArrayU32_getitem_next_jagged_project, uint32_t)
+ORACLE_JAGGED_PROJECT(awkward_MaskedArray64_getitem_next_jagged_project, int64_t)
+
+/* ======================================================================
  * Multi-core runner for the CPU baseline: run one reducer (any of the
  * (toptr, fromptr, offsets, outlength) family above, or argmax/argmin with
  * `starts`) over `nthreads` contiguous list ranges.  Each thread calls the

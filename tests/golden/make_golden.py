@@ -514,6 +514,73 @@ def layout_cases(rng, name):
     return out
 
 
+def sibling_cases(rng, name):
+    """Seeded inputs of the small siblings (adjust_starts_shifts, localindex,
+    range counts / spreads, missing-value jagged helpers)."""
+    rec = SIGNATURES[name]
+    fam = rec["family"]
+    args = {a[0]: a for a in rec["args"]}
+    S = 777
+    out = []
+    if fam == "awkward_NumpyArray_reduce_adjust_starts_shifts_64":
+        for n in (0, 1, 200):
+            starts = np.sort(rng.integers(0, 500, n)).astype(np.int64)
+            toptr = np.where(rng.random(n) < 0.2, -1, starts + rng.integers(0, 5, n)).astype(np.int64)
+            out.append({"toptr": toptr, "outlength": n, "offsets": np.zeros(n + 1, np.int64),
+                        "starts": starts, "shifts": rng.integers(0, 9, 600).astype(np.int64)})
+    elif fam == "awkward_localindex":
+        for n in (0, 1, 300):
+            out.append({"toindex": np.full(n, S, np.int64), "length": n})
+    elif fam == "awkward_ListArray_getitem_next_range_counts":
+        C = NP_DTYPES[args["fromoffsets"][1]]
+        for n in (0, 1, 150):
+            off = _offsets(_lengths(rng, n, 4, longs=(40,))) + 3
+            out.append({"total": np.full(1, S, np.int64), "fromoffsets": off.astype(C),
+                        "lenstarts": n})
+    elif fam == "awkward_ListArray_getitem_next_range_spreadadvanced":
+        C = NP_DTYPES[args["fromoffsets"][1]]
+        for n in (0, 1, 150):
+            off = _offsets(_lengths(rng, n, 4, longs=(40,)))
+            out.append({"toadvanced": np.full(int(off[-1]), S, np.int64),
+                        "fromadvanced": rng.integers(0, 1000, n).astype(np.int64),
+                        "fromoffsets": off.astype(C), "lenstarts": n})
+    elif fam == "awkward_RegularArray_getitem_next_range_spreadadvanced":
+        for length, size in ((0, 3), (4, 0), (90, 5), (30, 1)):
+            out.append({"toadvanced": np.full(length * size, S, np.int64),
+                        "fromadvanced": rng.integers(0, 1000, length).astype(np.int64),
+                        "length": length, "nextsize": size})
+    elif fam == "awkward_Content_getitem_next_missing_jagged_getmaskstartstop":
+        for n in (0, 1, 250):
+            idx = np.where(rng.random(n) < 0.3, -1, np.arange(n)).astype(np.int64)
+            valid = int((idx >= 0).sum())
+            offs = _offsets(_lengths(rng, valid, 3))
+            out.append({"index_in": idx, "offsets_in": offs, "mask_out": np.full(n, S, np.int64),
+                        "starts_out": np.full(n, S, np.int64), "stops_out": np.full(n, S, np.int64),
+                        "length": n})
+    elif fam == "awkward_MaskedArray_getitem_next_jagged_project":
+        T = NP_DTYPES[args["index"][1]]
+        for n in (0, 1, 250):
+            idx = rng.integers(0, 1000, n)
+            if T != np.uint32:
+                idx[rng.random(n) < 0.3] = -1
+            st = rng.integers(0, 500, n).astype(np.int64)
+            out.append({"index": idx.astype(T), "starts_in": st, "stops_in": st + rng.integers(0, 9, n),
+                        "starts_out": np.full(n, S, np.int64), "stops_out": np.full(n, S, np.int64),
+                        "length": n})
+    else:
+        raise KeyError(fam)
+    return out
+
+
+SIBLING_FAMILIES = (
+    "awkward_NumpyArray_reduce_adjust_starts_shifts_64", "awkward_localindex",
+    "awkward_ListArray_getitem_next_range_counts",
+    "awkward_ListArray_getitem_next_range_spreadadvanced",
+    "awkward_RegularArray_getitem_next_range_spreadadvanced",
+    "awkward_Content_getitem_next_missing_jagged_getmaskstartstop",
+    "awkward_MaskedArray_getitem_next_jagged_project")
+
+
 LAYOUT_FAMILIES = ("awkward_ListArray_compact_offsets", "awkward_RegularArray_getitem_carry",
                    "awkward_RegularArray_localindex")
 
@@ -540,6 +607,8 @@ def make_random():
             cases = complex_cases(rng, name)
         elif fam in LAYOUT_FAMILIES:
             cases = layout_cases(rng, name)
+        elif fam in SIBLING_FAMILIES:
+            cases = sibling_cases(rng, name)
         elif fam.startswith(NONLOCAL_PREFIXES):
             cases = nonlocal_cases(rng, name)
         elif fam == "awkward_RegularArray_combinations_64":
