@@ -56,9 +56,24 @@ __device__ __forceinline__ long long range_count(long long length, long long sta
   long long rs = start, re = stop;
   regularize_rangeslice(&rs, &re, step > 0, start != kSliceNone, stop != kSliceNone, length);
   *first = rs;
-  if (step > 0) return rs < re ? (re - rs - 1) / step + 1 : 0;
-  if (step < 0) return rs > re ? (rs - re - 1) / (-step) + 1 : 0;
-  return 0;
+  // |step| == 1 needs no division; otherwise a 32-bit one when the operands fit
+  // (64-bit division is a long software sequence)
+  long long span, astep;
+  if (step > 0) {
+    if (rs >= re) return 0;
+    span = re - rs - 1;
+    astep = step;
+  } else if (step < 0) {
+    if (rs <= re) return 0;
+    span = rs - re - 1;
+    astep = -step;
+  } else {
+    return 0;
+  }
+  if (astep == 1) return span + 1;
+  if (span < (1ll << 32) && astep < (1ll << 32))
+    return (long long)((unsigned)span / (unsigned)astep) + 1;
+  return span / astep + 1;
 }
 
 template <class C>
