@@ -415,6 +415,7 @@ struct ArgExtremumOp<double, MAX> {
 // Put the later cache sectors of a short run in flight before its loop walks
 // them (loads whose results are never read: nothing waits for them, so the
 // misses overlap instead of following one another).
+#pragma nv_diag_suppress 550  // the touch loads' destination is never read, by design
 __device__ __forceinline__ void touch_run(const void* p, int n, int esize) {
   const char* c = reinterpret_cast<const char*>(p);
   long long d;
@@ -422,6 +423,7 @@ __device__ __forceinline__ void touch_run(const void* p, int n, int esize) {
   if (n > 8) asm volatile("ld.global.nc.b64 %0, [%1];" : "=l"(d) : "l"(c + 8 * esize));
   if (n > 12) asm volatile("ld.global.nc.b64 %0, [%1];" : "=l"(d) : "l"(c + 12 * esize));
 }
+#pragma nv_diag_default 550
 
 // ---------------------------------------------------------------- short runs
 // Reduce n consecutive elements p[0..n) (global indices j0..j0+n) of one

@@ -493,7 +493,7 @@ __global__ void __launch_bounds__(kSortBlock)
          o0 += (long long)gridDim.x * kSortTile) {
       const long long lo = o0 / (2 * w) * (2 * w);
       const long long mid = lo + w < L ? lo + w : L, hi = lo + 2 * w < L ? lo + 2 * w : L;
-      const long long na = mid - lo, nb = hi - mid;
+      const long long na = mid - lo;
       const long long o1 = o0 + kSortTile < hi ? o0 + kSortTile : hi;
       const unsigned long long* ak = skey + base + lo;
       const long long* ai = sidx + base + lo;
