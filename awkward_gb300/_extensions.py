@@ -92,7 +92,7 @@ launches (capturable in a CUDA graph); plan_destroy frees the plan."""
 
 EXTENSIONS["awkward_gb300_batch_plan_create"] = (
     [("void**", "plan"), ("int64_t", "narrays"), ("const int64_t*", "nlists"),
-     ("const int64_t*", "nelements"), ("const double* const*", "x"),
+     ("const int64_t*", "nelements"), ("const int64_t*", "maxlen"), ("const double* const*", "x"),
      ("const int64_t* const*", "offsets"), ("const uint8_t* const*", "mask"),
      ("double* const*", "out_sum"), ("double* const*", "out_max"),
      ("int64_t* const*", "out_argmax"), ("int64_t* const*", "out_count"),

@@ -45,6 +45,10 @@ class Batch:
         ends = torch.stack([torch.stack([o[0], o[-1]]) for o, _c, _m in arrays]).cpu().numpy()
         self.nlists = np.array([o.numel() - 1 for o, _c, _m in arrays], np.int64)
         self.nelements = (ends[:, 1] - ends[:, 0]).astype(np.int64)
+        # longest list of each array (decides whether its reduction ranges may be widened)
+        self.maxlen = torch.stack([
+            (o[1:] - o[:-1]).max() if o.numel() > 1 else torch.zeros((), dtype=o.dtype, device=o.device)
+            for o, _c, _m in arrays]).cpu().numpy().astype(np.int64)
         self.out_sum, self.out_max, self.out_argmax, self.out_count = [], [], [], []
         self.sel_offsets, self.sel_content = [], []
         for (o, c, m), n in zip(arrays, self.nlists):
@@ -52,7 +56,8 @@ class Batch:
             self.out_max.append(torch.empty(max(n, 1), dtype=torch.float64, device=dev))
             self.out_argmax.append(torch.empty(max(n, 1), dtype=torch.int64, device=dev))
             self.out_count.append(torch.empty(max(n, 1), dtype=torch.int64, device=dev))
-            self.sel_offsets.append(torch.empty(n + 1, dtype=torch.int64, device=dev))
+            # zeroed: an array without lists has no select tile to write its offsets[0]
+            self.sel_offsets.append(torch.zeros(n + 1, dtype=torch.int64, device=dev))
             self.sel_content.append(torch.empty(max(c.numel(), 1), dtype=torch.float64, device=dev))
         self.err = torch.full((1,), -1, dtype=torch.int64, device=dev)
         self._plans = []
@@ -69,7 +74,7 @@ class Batch:
         return np.array([t.data_ptr() for t in tensors], np.uint64)
 
     def plan(self, order_mode=1, occupancy_div=1):
-        tables = [self.nlists, self.nelements,
+        tables = [self.nlists, self.nelements, self.maxlen,
                   self._ptrs([c for _o, c, _m in self.arrays]),
                   self._ptrs([o for o, _c, _m in self.arrays]),
                   self._ptrs([m for _o, _c, m in self.arrays]),

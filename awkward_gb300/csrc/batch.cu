@@ -260,14 +260,18 @@ cudaError_t upload(T** dst, const std::vector<T>& v) {
 
 }  // namespace
 
+constexpr long long kBatchMinRange = 4096;  // items per range when any split gives the same bits
+
 // Build a plan (set-up time: allocates and uploads its tables; synchronous).
 // Host arrays of length narrays: nlists, nelements (offsets[n] - offsets[0]),
-// and the device pointers of every array's content, offsets, mask and
+// maxlen (each array's longest list, -1 if unknown; may be null), and the
+// device pointers of every array's content, offsets, mask and
 // outputs.  order_mode 0: items in array order; 1: largest ranges first.
 // occupancy_div: persistent CTAs per SM = reducer occupancy / occupancy_div.
 // err_code: device word for bounded-wait failures of the select scan.
 GB_EXPORT int awkward_gb300_batch_plan_create(
     void** plan, int64_t narrays, const int64_t* nlists, const int64_t* nelements,
+    const int64_t* maxlen,
     const double* const* x, const int64_t* const* offsets, const uint8_t* const* mask,
     double* const* out_sum, double* const* out_max, int64_t* const* out_argmax,
     int64_t* const* out_count, int64_t* const* sel_offsets, double* const* sel_content,
@@ -292,8 +296,16 @@ GB_EXPORT int awkward_gb300_batch_plan_create(
     A.mask = mask[a];
     A.nlists = nlists[a];
     A.E = nelements[a] > 0 ? nelements[a] : 0;
+    // Lists of at most kAbsorb elements are reduced whole by the range where
+    // they end, so any split gives their bits: such arrays take ranges of at
+    // least kBatchMinRange items (fewer range searches per element).  An
+    // array with a longer list keeps its per-array split, whose partials the
+    // fix-up combines in the same order.
+    const bool any_split = maxlen != nullptr && maxlen[a] >= 0 && maxlen[a] <= kAbsorb;
     for (int k = 0; k < kOps; k++) {
-      A.ranges[k] = nlists[a] > 0 ? seg_ranges(nlists[a], A.E, W[k]) : 0;
+      A.ranges[k] = nlists[a] <= 0 ? 0
+                    : any_split ? seg_ranges_min(nlists[a], A.E, W[k], kBatchMinRange)
+                                : seg_ranges(nlists[a], A.E, W[k]);
       A.item0[k] = (int)items[k].size();
       for (int w = 0; w < A.ranges[k]; w++) items[k].push_back(make_int2(a, w));
     }

@@ -242,10 +242,14 @@ __device__ __forceinline__ void seg_reduce_range(const Op& op,
 // Number of warp ranges an array of nlists lists and E elements is split
 // into when W warps are available (the batched path uses the same split, so
 // both give bit-identical results).
-__host__ __device__ __forceinline__ int seg_ranges(long long nlists, long long E, int W) {
+__host__ __device__ __forceinline__ int seg_ranges_min(long long nlists, long long E, int W,
+                                                       long long min_items) {
   const long long D = nlists + E;
-  const long long wanted = (D + kMinRangeItems - 1) / kMinRangeItems;
+  const long long wanted = (D + min_items - 1) / min_items;
   return (int)(wanted < W ? wanted : W);
+}
+__host__ __device__ __forceinline__ int seg_ranges(long long nlists, long long E, int W) {
+  return seg_ranges_min(nlists, E, W, kMinRangeItems);
 }
 
 template <class Op>
