@@ -181,9 +181,16 @@ __global__ void __launch_bounds__(kTileBlock)
     for (int g = qa; g < qb; g += 32) {
       while (loc32[r + 1] <= g) r++;
       const int q = g + lane;
+      int rnext;
+      int rl = warp_step_lists(loc32, r, g, lane, &rnext);
+      if (rl < 0) {
+        rl = r;
+        if (q < qb)
+          while (loc32[rl + 1] <= q) rl++;
+        rnext = r;
+      }
+      r = rnext;
       if (q >= qb) continue;
-      int rl = r;
-      while (loc32[rl + 1] <= q) rl++;
       const int rank = q - loc32[rl];
       const long long s = s_size[rl];
       const long long base = s_start[rl];
@@ -243,9 +250,16 @@ __global__ void __launch_bounds__(kTileBlock)
   for (long long g = qa; g < qb; g += 32) {
     while (sm.loc[r + 1] <= g) r++;
     const long long q = g + lane;
+    int rnext;
+    int rl = warp_step_lists(sm.loc, r, g, lane, &rnext);
+    if (rl < 0) {
+      rl = r;
+      if (q < qb)
+        while (sm.loc[rl + 1] <= q) rl++;
+      rnext = r;
+    }
+    r = rnext;
     if (q >= qb) continue;
-    int rl = r;
-    while (sm.loc[rl + 1] <= q) rl++;
     long long rank = q - sm.loc[rl];
     const long long s = s_size[rl];
     const long long base = s_start[rl];

@@ -78,12 +78,45 @@ __device__ __forceinline__ int tile_find(const TileSmem& sm, long long q) {
   return lo;
 }
 
+// Lists of the 32 slots g .. g+31 of one warp step (all lanes call it).  r is
+// the list of slot g (the last list with loc[r] <= g).  Lane j gets the list
+// of slot g + j, and *rnext the list of slot g + 32.  The ends of lists
+// r .. r+31 are loaded one per lane; slot g + j lies in list
+// r + #{k : loc[r+1+k] <= g + j}.  Without empty lists among them the ends
+// in the step are distinct and that count is a popcount of their bitmask;
+// with empty ones a 5-step shuffle search over the sorted ends gives it.
+// Returns -1 on every lane when all 32 loaded lists end within the step.
+template <class T>
+__device__ __forceinline__ int warp_step_lists(const T* loc, int r, T g, int lane, int* rnext) {
+  constexpr unsigned kFull = 0xffffffffu;
+  const int k = r + 1 + lane;
+  int d = 33;  // distance of list r+lane's end from g (1..32 inside the step)
+  if (k <= kTileLists) {
+    const T diff = loc[k] - g;
+    if (diff <= 32) d = (int)diff;
+  }
+  const unsigned in = __ballot_sync(kFull, d <= 32);
+  if (in == kFull) return -1;
+  *rnext = r + __popc(in);
+  const unsigned ends = __reduce_or_sync(kFull, d <= 32 ? 1u << (d - 1) : 0u);
+  const int dn = __shfl_down_sync(kFull, d, 1);
+  if (!__any_sync(kFull, lane < 31 && d <= 32 && dn == d))
+    return r + __popc(ends & ((1u << lane) - 1u));
+  int c = 0;  // largest c with d[c-1] <= lane (d sorted; c <= 31 as in != kFull)
+#pragma unroll
+  for (int s = 16; s >= 1; s >>= 1) {
+    const int dv = __shfl_sync(kFull, d, c + s - 1);
+    if (dv <= lane) c += s;
+  }
+  return r + c;
+}
+
 // Visit every output slot q (0 <= q < total) of the tile with its list r.
 // With at least 4 slots per list on average each warp takes a contiguous
-// share, 32 consecutive slots per step (coalesced stores), and a lane finds
-// its list by walking forward from the list of the step's first slot; with
-// fewer a 32-slot step spans many lists, and a binary search per slot is
-// shorter than the walk.
+// share, 32 consecutive slots per step (coalesced stores), and the lanes find
+// their lists from the list of the step's first slot (warp_step_lists; a
+// forward walk when more than 31 lists end inside one step); with fewer a
+// 32-slot step spans many lists, and a binary search per slot is shorter.
 template <class F>
 __device__ __forceinline__ void tile_for_each_slot(const TileSmem& sm, long long total, F fn) {
   if (total < 4ll * kTileLists) {
@@ -98,11 +131,16 @@ __device__ __forceinline__ void tile_for_each_slot(const TileSmem& sm, long long
   for (long long g = qa; g < qb; g += 32) {
     while (sm.loc[r + 1] <= g) r++;
     const long long q = g + lane;
-    if (q < qb) {
-      int rl = r;
-      while (sm.loc[rl + 1] <= q) rl++;
-      fn(q, rl);
+    int rnext;
+    int rl = warp_step_lists(sm.loc, r, g, lane, &rnext);
+    if (rl < 0) {
+      rl = r;
+      if (q < qb)
+        while (sm.loc[rl + 1] <= q) rl++;
+      rnext = r;
     }
+    if (q < qb) fn(q, rl);
+    r = rnext;
   }
 }
 

@@ -21,10 +21,10 @@ import oracle
 pytestmark = pytest.mark.gpu
 
 
-def _case(nl, seed, lam=8, base=0, extra=None, p=0.4):
+def _case(nl, seed, lam=8, base=0, extra=None, p=0.4, pe=0.01):
     rng = np.random.default_rng(seed)
     L = rng.poisson(lam, nl)
-    L[rng.random(nl) < 0.01] = 0
+    L[rng.random(nl) < pe] = 0
     if extra is not None:
         L = np.concatenate([L, extra])
     off = (np.concatenate([[0], np.cumsum(L)]) + base).astype(np.int64)
@@ -35,21 +35,25 @@ def _case(nl, seed, lam=8, base=0, extra=None, p=0.4):
 
 def _np_mask_index(off, mask):
     L = np.diff(off)
-    counts = np.add.reduceat(mask[off[0]:].astype(np.int64), off[:-1] - off[0]) * (L > 0) if len(L) else np.zeros(0, np.int64)
+    cs = np.concatenate([[0], np.cumsum(mask[off[0]:].astype(np.int64))])
+    counts = cs[off[1:] - off[0]] - cs[off[:-1] - off[0]]
     ioff = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
     owner = np.repeat(np.arange(len(L)), L)
     local = np.arange(int(off[-1] - off[0])) - (off[:-1] - off[0])[owner]
     return ioff, local[mask[off[0]:]].astype(np.int64)
 
 
-@pytest.mark.parametrize("variant", ["poisson", "base", "all_true", "all_false", "long_list"])
+@pytest.mark.parametrize("variant", ["poisson", "base", "all_true", "all_false", "long_list",
+                                     "short", "half_empty"])
 def test_mask_to_index_matches_numpy(variant):
     import torch
 
     from awkward_gb300 import jagged
 
     kw = {"poisson": {}, "base": {"base": 7}, "all_true": {"p": 1.1}, "all_false": {"p": -1},
-          "long_list": {"extra": np.array([0, 100_000, 3])}}[variant]
+          "long_list": {"extra": np.array([0, 100_000, 3])},
+          # more than 31 lists ending in one 32-element step; runs of empty lists
+          "short": {"lam": 0.4}, "half_empty": {"pe": 0.5}}[variant]
     _rng, _L, off, _x, mask = _case(50_000, 11, **kw)
     ioff, idx = jagged.jagged_mask_to_index(torch.from_numpy(off).cuda(),
                                             torch.from_numpy(mask).cuda())
