@@ -9,10 +9,13 @@
 //
 // mask_to_index: one CTA per tile of kTileLists lists.  Thread-per-list counts
 // of true entries are scanned across tiles (decoupled look-back) into the new
-// offsets; then each warp walks a contiguous share of the tile's elements 32
-// at a time, ranking the true entries with a ballot prefix, and writes the
-// local index (position within its list) of every true entry at its rank, so
-// both passes over the mask and the index writes are coalesced.
+// offsets.  A tile of at most kMaskBits elements is first staged as a bitmap
+// in shared memory (16-byte loads); the counts are popcounts of it, each
+// thread lists its lists' true positions in rank order in shared memory, and
+// the tile's positions are copied out coalesced.  A larger tile counts from
+// global memory and then each warp walks a contiguous share of its elements
+// 32 at a time, ranking the true entries with a ballot prefix and writing the
+// local index (position within its list) of each at its rank.
 #include "list_tile.cuh"
 
 using namespace gb;
@@ -25,12 +28,46 @@ struct MaskTile {
   int count;
 };
 
+// A tile whose mask bytes (plus the first byte's offset in its 16-byte line)
+// fit kMaskBits is staged as a bitmap in shared memory; its true entries'
+// positions are gathered there in rank order and copied out coalesced.
+constexpr int kMaskBits = 16384;
+struct MaskStage {
+  unsigned bits[kMaskBits / 32];   // bit p: byte (tile's first byte - shift + p) is nonzero
+  unsigned short pos[kMaskBits];   // position within its list of each true entry, by rank
+};
+
+// 4 mask bytes -> 4 bits (byte k nonzero -> bit k).  Bit 7 of each byte of
+// ((w & 0x7f..) + 0x7f..) | w is set iff the byte is nonzero (no carries
+// between bytes); the multiply gathers the four bit-7s into bits 21..24.
+__device__ __forceinline__ unsigned nonzero_nibble(unsigned w) {
+  const unsigned hi = ((((w & 0x7f7f7f7fu) + 0x7f7f7f7fu) | w) & 0x80808080u) >> 7;
+  return (hi * 0x00204081u) >> 21 & 0xfu;
+}
+__device__ __forceinline__ unsigned nonzero_bits16(uint4 v) {
+  return nonzero_nibble(v.x) | nonzero_nibble(v.y) << 4 | nonzero_nibble(v.z) << 8 |
+         nonzero_nibble(v.w) << 12;
+}
+
+// Set bits of bits[] in the bit range [a, b).
+__device__ __forceinline__ int bitmap_count(const unsigned* bits, int a, int b) {
+  if (a >= b) return 0;
+  int w = a >> 5;
+  const int we = b >> 5;
+  if (w == we) return __popc(bits[w] & ((1u << (b & 31)) - 1u) & ~((1u << (a & 31)) - 1u));
+  int n = __popc(bits[w] >> (a & 31));
+  for (w++; w < we; w++) n += __popc(bits[w]);
+  if (b & 31) n += __popc(bits[we] & ((1u << (b & 31)) - 1u));
+  return n;
+}
+
 __global__ void __launch_bounds__(kTileBlock)
     mask_to_index_kernel(int64_t* __restrict__ tooffsets, int64_t* __restrict__ toindex,
                          const uint8_t* __restrict__ mask, const int64_t* __restrict__ offsets,
                          long long nlists, long long ntiles, ScanTiles st, uint64_t* err) {
   __shared__ TileSmem sm;
   __shared__ MaskTile t;
+  __shared__ MaskStage ms;
   const long long tile = tile_claim(sm, st);
   const long long l0 = tile * kTileLists;
   const long long rem = nlists - l0;
@@ -45,23 +82,77 @@ __global__ void __launch_bounds__(kTileBlock)
     t.count = count;
   }
   __syncthreads();
+  const long long total = t.loc[count];
+  const uint8_t* p0 = mask + base;
+  const int sh = (int)(reinterpret_cast<uintptr_t>(p0) & 15);
+  const bool staged = total + sh <= kMaskBits;
   long long c[kTileLPT];
+  if (staged) {
+    // bitmap of the tile's bytes: 32 bytes per word, two aligned 16-byte loads
+    // for words inside [p0, p0 + total), byte loads for the partial ends
+    const int nbits = (int)total + sh;
+    const uint8_t* a0 = p0 - sh;
+    for (int w = threadIdx.x; w < (nbits + 31) >> 5; w += kTileBlock) {
+      const int lo = 32 * w, hi = lo + 32;
+      unsigned word = 0;
+      if (lo >= sh && hi <= nbits) {
+        const uint4 v0 = __ldg(reinterpret_cast<const uint4*>(a0 + lo));
+        const uint4 v1 = __ldg(reinterpret_cast<const uint4*>(a0 + lo + 16));
+        word = nonzero_bits16(v0) | nonzero_bits16(v1) << 16;
+      } else {
+        const int b0 = lo > sh ? lo : sh, b1 = hi < nbits ? hi : nbits;
+        for (int b = b0; b < b1; b++) word |= (unsigned)(a0[b] != 0) << (b - lo);
+      }
+      ms.bits[w] = word;
+    }
+    __syncthreads();
 #pragma unroll
-  for (int r = 0; r < kTileLPT; r++) {
-    const int li = threadIdx.x * kTileLPT + r;
-    long long n = 0;
-    if (li < count)
-      for (long long j = base + t.loc[li]; j < base + t.loc[li + 1]; j++) n += mask[j] != 0;
-    c[r] = n;
+    for (int r = 0; r < kTileLPT; r++) {
+      const int li = threadIdx.x * kTileLPT + r;
+      c[r] = li < count ? bitmap_count(ms.bits, (int)t.loc[li] + sh, (int)t.loc[li + 1] + sh) : 0;
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < kTileLPT; r++) {
+      const int li = threadIdx.x * kTileLPT + r;
+      long long n = 0;
+      if (li < count)
+        for (long long j = base + t.loc[li]; j < base + t.loc[li + 1]; j++) n += mask[j] != 0;
+      c[r] = n;
+    }
   }
   const long long prefix = tile_scan(sm, st, tile, c, 0, err);
   for (int li = threadIdx.x; li < kTileLists; li += kTileBlock)
     if (li < count) tooffsets[l0 + li] = prefix + sm.loc[li];
   if (tile == ntiles - 1 && threadIdx.x == 0) tooffsets[nlists] = prefix + sm.total;
-  // element pass
+  if (staged) {
+    // each thread lists its lists' true entries in rank order, then the tile's
+    // positions are copied out with consecutive threads on consecutive ranks
+#pragma unroll
+    for (int r = 0; r < kTileLPT; r++) {
+      const int li = threadIdx.x * kTileLPT + r;
+      if (li >= count || c[r] == 0) continue;
+      const int a = (int)t.loc[li] + sh, b = (int)t.loc[li + 1] + sh;
+      int o = (int)sm.loc[li];
+      for (int w = a >> 5; w <= (b - 1) >> 5; w++) {
+        unsigned word = ms.bits[w];
+        if (w == a >> 5) word &= ~((1u << (a & 31)) - 1u);
+        if (w == b >> 5) word &= (1u << (b & 31)) - 1u;
+        while (word) {
+          const int bit = __ffs(word) - 1;
+          word &= word - 1;
+          ms.pos[o++] = (unsigned short)(32 * w + bit - a);
+        }
+      }
+    }
+    __syncthreads();
+    const int ntrue = (int)sm.total;
+    for (int i = threadIdx.x; i < ntrue; i += kTileBlock) toindex[prefix + i] = ms.pos[i];
+    return;
+  }
+  // element pass of a tile with long lists
   constexpr int kWarps = kTileBlock / 32;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long total = t.loc[count];
   const long long qa = total * warp / kWarps, qb = total * (warp + 1) / kWarps;
   if (qa >= qb) return;
   int lo = 0, hi = count;  // list holding element qa: last r with loc[r] <= qa

@@ -8,9 +8,10 @@
 // its lengths in shared memory, obtains the tile's global prefix with a
 // decoupled look-back (single pass, bounded spins), writes its offsets, and
 // then fills its outputs in output order -- each warp a contiguous share of
-// the tile's slots, consecutive lanes on consecutive slots, each slot finding
-// its list by a forward walk over the tile's local offsets.  The fill is
-// therefore coalesced and balanced inside the tile regardless of list lengths.
+// the tile's slots, consecutive lanes on consecutive slots, the lanes of a
+// step finding their lists together from the tile's local offsets.  The fill
+// is therefore coalesced and balanced inside the tile regardless of list
+// lengths.
 #pragma once
 
 #include "gb_common.cuh"
@@ -112,14 +113,15 @@ __device__ __forceinline__ int warp_step_lists(const T* loc, int r, T g, int lan
 }
 
 // Visit every output slot q (0 <= q < total) of the tile with its list r.
-// With at least 4 slots per list on average each warp takes a contiguous
+// With at least 1.5 slots per list on average each warp takes a contiguous
 // share, 32 consecutive slots per step (coalesced stores), and the lanes find
 // their lists from the list of the step's first slot (warp_step_lists; a
 // forward walk when more than 31 lists end inside one step); with fewer a
-// 32-slot step spans many lists, and a binary search per slot is shorter.
+// 32-slot step often spans more than 32 lists, and a binary search per slot
+// is shorter.
 template <class F>
 __device__ __forceinline__ void tile_for_each_slot(const TileSmem& sm, long long total, F fn) {
-  if (total < 4ll * kTileLists) {
+  if (total < (long long)(kTileLists + kTileLists / 2)) {
     for (long long q = threadIdx.x; q < total; q += kTileBlock) fn(q, tile_find(sm, q));
     return;
   }

@@ -44,7 +44,7 @@ def _np_mask_index(off, mask):
 
 
 @pytest.mark.parametrize("variant", ["poisson", "base", "all_true", "all_false", "long_list",
-                                     "short", "half_empty"])
+                                     "short", "half_empty", "tile_cap"])
 def test_mask_to_index_matches_numpy(variant):
     import torch
 
@@ -53,7 +53,9 @@ def test_mask_to_index_matches_numpy(variant):
     kw = {"poisson": {}, "base": {"base": 7}, "all_true": {"p": 1.1}, "all_false": {"p": -1},
           "long_list": {"extra": np.array([0, 100_000, 3])},
           # more than 31 lists ending in one 32-element step; runs of empty lists
-          "short": {"lam": 0.4}, "half_empty": {"pe": 0.5}}[variant]
+          "short": {"lam": 0.4}, "half_empty": {"pe": 0.5},
+          # tiles of 1024 lists on both sides of the 16384-element staging limit
+          "tile_cap": {"lam": 16}}[variant]
     _rng, _L, off, _x, mask = _case(50_000, 11, **kw)
     ioff, idx = jagged.jagged_mask_to_index(torch.from_numpy(off).cuda(),
                                             torch.from_numpy(mask).cuda())
