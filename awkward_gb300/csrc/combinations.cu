@@ -7,9 +7,9 @@
 // The CPU enumerates each list's tuples depth-first in lexicographic order.
 // Here every output slot is produced independently: a list tile scans the
 // per-list tuple counts (decoupled look-back), then each warp fills a
-// contiguous share of the tile's slots, 32 consecutive slots per step; a lane
-// finds its list by walking forward from the list of the step's first slot
-// and unranks the slot's lexicographic rank into the tuple (combinatorial
+// contiguous share of the tile's slots, 32 consecutive slots per step; the
+// lanes find their lists from the list of the step's first slot, and each
+// unranks the slot's lexicographic rank into the tuple (combinatorial
 // number system: closed forms for n = 1, 2, 3; for larger n each position by
 // bisection over "tuples whose next element is below v" = C(s-lo, rem) -
 // C(s-v, rem)).  With replacement the non-decreasing tuple over s elements is
@@ -160,8 +160,8 @@ __global__ void __launch_bounds__(kTileBlock)
     for (long long p = threadIdx.x; p < n; p += kTileBlock) toindex[p] = prefix + total;
   if (n <= 0) return;
   // Each warp fills a contiguous share of the tile's tuples, 32 consecutive
-  // output slots per step (coalesced stores); a lane finds its list by
-  // walking forward from the list of the step's first slot.
+  // output slots per step (coalesced stores); the lanes find their lists
+  // from the list of the step's first slot (warp_step_lists).
   constexpr int kWarps = kTileBlock / 32;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if ((n == 2 || n == 3) && total < (1ll << 31)) {
