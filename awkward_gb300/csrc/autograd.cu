@@ -9,12 +9,15 @@
 //                      d x_j = y_j (g_j - sum_k g_k y_k)         (fused Jacobian product)
 // The forward sum and max use the segmented reducers of this library.
 //
-// Layout: a CTA owns a tile of kTileLists consecutive lists.  It stages the
-// tile's offsets in shared memory, computes per-list statistics (max, sums)
-// with one thread per list where a pass needs them, and then visits the
-// tile's elements in order -- consecutive threads on consecutive elements,
-// each finding its list by a short forward walk over the staged offsets -- so
-// every element-sized read and write is coalesced.
+// Layout: a CTA owns a tile of kSoftLists consecutive lists, one thread per
+// list.  It stages the tile's offsets and, when the tile's elements fit
+// (kSoftBytes per array), the element arrays it reads more than once in
+// shared memory with coalesced loads, plus an element -> list map (one byte
+// per element).  Per-list statistics (max, sums) are computed by one thread
+// per list in element order, from shared memory; then the tile's elements are
+// visited with consecutive threads on consecutive elements, so every global
+// read and write is coalesced.  A tile whose elements do not fit reads them
+// from global memory and finds each element's list by binary search.
 #include <math.h>
 
 #include "list_tile.cuh"
@@ -33,19 +36,26 @@ __device__ __forceinline__ double exp_t<double>(double v) { return exp(v); }
 template <class T>
 __device__ __forceinline__ T max_t(T a, T b) { return a > b ? a : b; }
 
-struct TileLists {
-  long long loc[kTileLists + 1];  // offsets of the tile's lists, relative to its first element
+constexpr int kSoftLists = 128;       // lists (and threads) per CTA
+constexpr int kSoftBytes = 16384;     // staging per element array
+constexpr int kSoftElems = 4096;      // element -> list map entries (>= kSoftBytes / 4)
+
+struct SoftTile {
+  long long loc[kSoftLists + 1];  // offsets of the tile's lists, relative to its first element
+  unsigned char owner[kSoftElems];
   long long base;                 // first element of the tile
   int count;                      // lists in this tile
+  int mapped;                     // owner[] holds every element's list
 };
 
-// Stage offsets[l0 .. l0+count] (all threads; ends with __syncthreads).
-__device__ __forceinline__ void stage_tile(TileLists& t, const int64_t* __restrict__ offsets,
-                                           long long l0, long long nlists) {
+// Stage offsets[l0 .. l0+count] and, if the tile has at most `cap` elements,
+// the element -> list map (all threads; ends with __syncthreads).
+__device__ __forceinline__ void stage_soft_tile(SoftTile& t, const int64_t* __restrict__ offsets,
+                                                long long l0, long long nlists, int cap) {
   const long long rem = nlists - l0;
-  const int count = (int)(rem < kTileLists ? rem : kTileLists);
+  const int count = (int)(rem < kSoftLists ? rem : kSoftLists);
   const long long base = __ldg(offsets + l0);
-  for (int i = threadIdx.x; i <= kTileLists; i += blockDim.x) {
+  for (int i = threadIdx.x; i <= kSoftLists; i += blockDim.x) {
     const int k = i < count ? i : count;
     t.loc[i] = __ldg(offsets + l0 + k) - base;
   }
@@ -54,43 +64,85 @@ __device__ __forceinline__ void stage_tile(TileLists& t, const int64_t* __restri
     t.count = count;
   }
   __syncthreads();
+  const bool mapped = t.loc[count] <= cap;
+  if (mapped && (int)threadIdx.x < count) {
+    const int a = (int)t.loc[threadIdx.x], b = (int)t.loc[threadIdx.x + 1];
+    for (int q = a; q < b; q++) t.owner[q] = (unsigned char)threadIdx.x;
+  }
+  if (threadIdx.x == 0) t.mapped = mapped ? 1 : 0;
+  __syncthreads();
 }
 
-// Visit every element of the tile in order: fn(element index, local list).
-// Each warp takes a contiguous share, 32 consecutive elements per step.
-template <class F>
-__device__ __forceinline__ void for_tile_elements(const TileLists& t, F fn) {
-  constexpr int kWarps = kTileBlock / 32;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long total = t.loc[t.count];
-  const long long qa = total * warp / kWarps, qb = total * (warp + 1) / kWarps;
-  if (qa >= qb) return;
-  int lo = 0, hi = t.count;  // last r with loc[r] <= qa
+// List of tile element q: the map, or the last r with loc[r] <= q.
+__device__ __forceinline__ int soft_list(const SoftTile& t, long long q) {
+  if (t.mapped) return t.owner[q];
+  int lo = 0, hi = t.count;
   while (hi - lo > 1) {
     const int mid = (lo + hi) >> 1;
-    if (t.loc[mid] <= qa) lo = mid;
+    if (t.loc[mid] <= q) lo = mid;
     else hi = mid;
   }
-  int r = lo;
-  for (long long g = qa; g < qb; g += 32) {
-    while (t.loc[r + 1] <= g) r++;
-    const long long q = g + lane;
-    if (q >= qb) continue;
-    int rl = r;
-    while (t.loc[rl + 1] <= q) rl++;
-    fn(t.base + q, rl);
+  return lo;
+}
+
+// Copy src[0 .. n) to dst (shared memory), four loads in flight per thread.
+template <class T>
+__device__ __forceinline__ void stage_elements(T* dst, const T* __restrict__ src, long long n) {
+  const int nb = blockDim.x;
+  for (long long q0 = threadIdx.x; q0 < n; q0 += 4ll * nb) {
+    T v[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const long long q = q0 + (long long)k * nb;
+      v[k] = q < n ? __ldg(src + q) : T(0);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const long long q = q0 + (long long)k * nb;
+      if (q < n) dst[q] = v[k];
+    }
   }
+}
+
+// The same for two arrays at once (eight loads in flight per thread).
+template <class T>
+__device__ __forceinline__ void stage_elements2(T* dst0, const T* __restrict__ src0, T* dst1,
+                                                const T* __restrict__ src1, long long n) {
+  const int nb = blockDim.x;
+  for (long long q0 = threadIdx.x; q0 < n; q0 += 4ll * nb) {
+    T v[4], w[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const long long q = q0 + (long long)k * nb;
+      v[k] = q < n ? __ldg(src0 + q) : T(0);
+      w[k] = q < n ? __ldg(src1 + q) : T(0);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      const long long q = q0 + (long long)k * nb;
+      if (q < n) {
+        dst0[q] = v[k];
+        dst1[q] = w[k];
+      }
+    }
+  }
+}
+
+inline unsigned soft_tiles(long long nlists) {
+  return (unsigned)((nlists + kSoftLists - 1) / kSoftLists);
 }
 
 // ---------------------------------------------------------------- sum backward
 template <class T>
-__global__ void __launch_bounds__(kTileBlock)
+__global__ void __launch_bounds__(kSoftLists)
     sum_backward_kernel(T* __restrict__ gx, const T* __restrict__ gout,
                         const int64_t* __restrict__ offsets, long long nlists) {
-  __shared__ TileLists t;
-  const long long l0 = (long long)blockIdx.x * kTileLists;
-  stage_tile(t, offsets, l0, nlists);
-  for_tile_elements(t, [&](long long j, int r) { gx[j] = __ldg(gout + l0 + r); });
+  __shared__ SoftTile t;
+  const long long l0 = (long long)blockIdx.x * kSoftLists;
+  stage_soft_tile(t, offsets, l0, nlists, kSoftElems);
+  const long long total = t.loc[t.count];
+  for (long long q = threadIdx.x; q < total; q += blockDim.x)
+    gx[t.base + q] = __ldg(gout + l0 + soft_list(t, q));
 }
 
 // ---------------------------------------------------------------- max backward
@@ -108,82 +160,100 @@ __global__ void max_backward_kernel(T* __restrict__ gx, const T* __restrict__ go
 }
 
 // ---------------------------------------------------------------- softmax
-// Per-list max and sum of exp(x - max) by one thread per list.
 template <class T>
-__device__ __forceinline__ void list_stats(const T* __restrict__ x, const TileLists& t,
-                                           T* s_max, T* s_sum) {
-  for (int r = threadIdx.x; r < t.count; r += blockDim.x) {
-    const T* p = x + t.base + t.loc[r];
-    const long long n = t.loc[r + 1] - t.loc[r];
-    T m = -INFINITY;
-    for (long long i = 0; i < n; i++) m = max_t(m, p[i]);
-    T s = 0;
-    for (long long i = 0; i < n; i++) s += exp_t(p[i] - m);
-    s_max[r] = m;
-    s_sum[r] = s;
-  }
-}
-
-template <class T>
-__global__ void __launch_bounds__(kTileBlock)
+__global__ void __launch_bounds__(kSoftLists)
     softmax_forward_kernel(T* __restrict__ y, const T* __restrict__ x,
                            const int64_t* __restrict__ offsets, long long nlists) {
-  __shared__ TileLists t;
-  __shared__ T s_max[kTileLists];
-  __shared__ T s_sum[kTileLists];
-  const long long l0 = (long long)blockIdx.x * kTileLists;
-  stage_tile(t, offsets, l0, nlists);
-  list_stats(x, t, s_max, s_sum);
+  constexpr int cap = kSoftBytes / (int)sizeof(T);
+  __shared__ SoftTile t;
+  __shared__ T sx[cap];
+  __shared__ T s_max[kSoftLists];
+  __shared__ T s_sum[kSoftLists];
+  const long long l0 = (long long)blockIdx.x * kSoftLists;
+  stage_soft_tile(t, offsets, l0, nlists, cap);
+  const long long total = t.loc[t.count];
+  if (t.mapped) {
+    stage_elements(sx, x + t.base, total);
+    __syncthreads();
+  }
+  const T* xs = t.mapped ? sx : x + t.base;
+  const int r = threadIdx.x;
+  if (r < t.count) {  // per-list max and sum of exp(x - max)
+    const long long a = t.loc[r], b = t.loc[r + 1];
+    T m = -INFINITY;
+    for (long long q = a; q < b; q++) m = max_t(m, xs[q]);
+    T sum = 0;
+    for (long long q = a; q < b; q++) sum += exp_t(xs[q] - m);
+    s_max[r] = m;
+    s_sum[r] = sum;
+  }
   __syncthreads();
-  for_tile_elements(t, [&](long long j, int r) { y[j] = exp_t(x[j] - s_max[r]) / s_sum[r]; });
+  for (long long q = threadIdx.x; q < total; q += blockDim.x) {
+    const int l = soft_list(t, q);
+    y[t.base + q] = exp_t(xs[q] - s_max[l]) / s_sum[l];
+  }
 }
 
 // d x_j = y_j (g_j - sum_k g_k y_k); y from `ysaved` when given, else
 // recomputed from x (max and normaliser recomputed per list).
 template <class T>
-__global__ void __launch_bounds__(kTileBlock)
+__global__ void __launch_bounds__(kSoftLists)
     softmax_backward_kernel(T* __restrict__ gx, const T* __restrict__ gy,
                             const T* __restrict__ x, const T* __restrict__ ysaved,
                             const int64_t* __restrict__ offsets, long long nlists) {
-  __shared__ TileLists t;
-  __shared__ T s_max[kTileLists];
-  __shared__ T s_sum[kTileLists];
-  __shared__ T s_dot[kTileLists];
-  const long long l0 = (long long)blockIdx.x * kTileLists;
-  stage_tile(t, offsets, l0, nlists);
+  constexpr int cap = kSoftBytes / (int)sizeof(T);
+  __shared__ SoftTile t;
+  __shared__ T sa[cap];  // x, or the saved y
+  __shared__ T sg[cap];  // gy
+  __shared__ T s_max[kSoftLists];
+  __shared__ T s_sum[kSoftLists];
+  __shared__ T s_dot[kSoftLists];
+  const long long l0 = (long long)blockIdx.x * kSoftLists;
+  stage_soft_tile(t, offsets, l0, nlists, cap);
+  const long long total = t.loc[t.count];
+  const T* src = ysaved ? ysaved : x;
+  if (t.mapped) {
+    stage_elements2(sa, src + t.base, sg, gy + t.base, total);
+    __syncthreads();
+  }
+  const T* as = t.mapped ? sa : src + t.base;
+  const T* gs = t.mapped ? sg : gy + t.base;
+  const int r = threadIdx.x;
   if (ysaved) {
-    for (int r = threadIdx.x; r < t.count; r += blockDim.x) {
-      const long long a = t.base + t.loc[r], b = t.base + t.loc[r + 1];
+    if (r < t.count) {
+      const long long a = t.loc[r], b = t.loc[r + 1];
       T d = 0;
-      for (long long j = a; j < b; j++) d += gy[j] * ysaved[j];
+      for (long long q = a; q < b; q++) d += gs[q] * as[q];
       s_dot[r] = d;
     }
     __syncthreads();
-    for_tile_elements(t, [&](long long j, int r) { gx[j] = ysaved[j] * (gy[j] - s_dot[r]); });
+    for (long long q = threadIdx.x; q < total; q += blockDim.x) {
+      const int l = soft_list(t, q);
+      gx[t.base + q] = as[q] * (gs[q] - s_dot[l]);
+    }
     return;
   }
-  for (int r = threadIdx.x; r < t.count; r += blockDim.x) {
-    const long long a = t.base + t.loc[r], b = t.base + t.loc[r + 1];
+  if (r < t.count) {
+    const long long a = t.loc[r], b = t.loc[r + 1];
     T m = -INFINITY;
-    for (long long j = a; j < b; j++) m = max_t(m, x[j]);
-    T s = 0, gs = 0;
-    for (long long j = a; j < b; j++) {
-      const T e = exp_t(x[j] - m);
-      s += e;
-      gs += gy[j] * e;
+    for (long long q = a; q < b; q++) m = max_t(m, as[q]);
+    T sum = 0, gsum = 0;
+    for (long long q = a; q < b; q++) {
+      const T e = exp_t(as[q] - m);
+      sum += e;
+      gsum += gs[q] * e;
     }
     s_max[r] = m;
-    s_sum[r] = s;
-    s_dot[r] = gs / s;
+    s_sum[r] = sum;
+    s_dot[r] = gsum / sum;
   }
   __syncthreads();
-  for_tile_elements(t, [&](long long j, int r) {
-    const T yj = exp_t(x[j] - s_max[r]) / s_sum[r];
-    gx[j] = yj * (gy[j] - s_dot[r]);
-  });
+  for (long long q = threadIdx.x; q < total; q += blockDim.x) {
+    const int l = soft_list(t, q);
+    const T yj = exp_t(as[q] - s_max[l]) / s_sum[l];
+    gx[t.base + q] = yj * (gs[q] - s_dot[l]);
+  }
 }
-
-inline unsigned tiles_of(long long nlists) { return (unsigned)tile_count(nlists); }
 
 }  // namespace
 
@@ -192,7 +262,7 @@ inline unsigned tiles_of(long long nlists) { return (unsigned)tile_count(nlists)
   GB_EXPORT int awkward_gb300_segment_sum_backward_##SUFFIX(                                    \
       T* grad_x, const T* grad_out, const int64_t* offsets, int64_t nlists, void* stream) {    \
     if (nlists <= 0) return 0;                                                                  \
-    sum_backward_kernel<T><<<tiles_of(nlists), kTileBlock, 0, (cudaStream_t)stream>>>(         \
+    sum_backward_kernel<T><<<soft_tiles(nlists), kSoftLists, 0, (cudaStream_t)stream>>>(         \
         grad_x, grad_out, offsets, nlists);                                                     \
     return (int)cudaGetLastError();                                                             \
   }                                                                                             \
@@ -214,7 +284,7 @@ inline unsigned tiles_of(long long nlists) { return (unsigned)tile_count(nlists)
   GB_EXPORT int awkward_gb300_jagged_softmax_forward_##SUFFIX(                                  \
       T* y, const T* x, const int64_t* offsets, int64_t nlists, void* stream) {                \
     if (nlists <= 0) return 0;                                                                  \
-    softmax_forward_kernel<T><<<tiles_of(nlists), kTileBlock, 0, (cudaStream_t)stream>>>(      \
+    softmax_forward_kernel<T><<<soft_tiles(nlists), kSoftLists, 0, (cudaStream_t)stream>>>(      \
         y, x, offsets, nlists);                                                                 \
     return (int)cudaGetLastError();                                                             \
   }                                                                                             \
@@ -222,7 +292,7 @@ inline unsigned tiles_of(long long nlists) { return (unsigned)tile_count(nlists)
       T* grad_x, const T* grad_y, const T* x, const T* y_saved, const int64_t* offsets,        \
       int64_t nlists, void* stream) {                                                           \
     if (nlists <= 0) return 0;                                                                  \
-    softmax_backward_kernel<T><<<tiles_of(nlists), kTileBlock, 0, (cudaStream_t)stream>>>(     \
+    softmax_backward_kernel<T><<<soft_tiles(nlists), kSoftLists, 0, (cudaStream_t)stream>>>(     \
         grad_x, grad_y, x, y_saved, offsets, nlists);                                           \
     return (int)cudaGetLastError();                                                             \
   }
