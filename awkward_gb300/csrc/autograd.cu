@@ -9,8 +9,8 @@
 //                      d x_j = y_j (g_j - sum_k g_k y_k)         (fused Jacobian product)
 // The forward sum and max use the segmented reducers of this library.
 //
-// Layout: a CTA owns a tile of kSoftLists consecutive lists, one thread per
-// list.  It stages the tile's offsets and, when the tile's elements fit
+// Layout: a CTA owns a tile of kSoftLists consecutive lists, one statistics
+// thread per list, and twice as many threads for the memory passes.  It stages the tile's offsets and, when the tile's elements fit
 // (kSoftBytes per array), the element arrays it reads more than once in
 // shared memory with coalesced loads, plus an element -> list map (one byte
 // per element).  Per-list statistics (max, sums) are computed by one thread
@@ -36,7 +36,8 @@ __device__ __forceinline__ double exp_t<double>(double v) { return exp(v); }
 template <class T>
 __device__ __forceinline__ T max_t(T a, T b) { return a > b ? a : b; }
 
-constexpr int kSoftLists = 128;       // lists (and threads) per CTA
+constexpr int kSoftLists = 128;       // lists per CTA (one statistics thread each)
+constexpr int kSoftThreads = 256;     // threads per CTA (staging and element passes)
 constexpr int kSoftBytes = 16384;     // staging per element array
 constexpr int kSoftElems = 4096;      // element -> list map entries (>= kSoftBytes / 4)
 
@@ -134,7 +135,7 @@ inline unsigned soft_tiles(long long nlists) {
 
 // ---------------------------------------------------------------- sum backward
 template <class T>
-__global__ void __launch_bounds__(kSoftLists)
+__global__ void __launch_bounds__(kSoftThreads)
     sum_backward_kernel(T* __restrict__ gx, const T* __restrict__ gout,
                         const int64_t* __restrict__ offsets, long long nlists) {
   __shared__ SoftTile t;
@@ -161,7 +162,7 @@ __global__ void max_backward_kernel(T* __restrict__ gx, const T* __restrict__ go
 
 // ---------------------------------------------------------------- softmax
 template <class T>
-__global__ void __launch_bounds__(kSoftLists)
+__global__ void __launch_bounds__(kSoftThreads)
     softmax_forward_kernel(T* __restrict__ y, const T* __restrict__ x,
                            const int64_t* __restrict__ offsets, long long nlists) {
   constexpr int cap = kSoftBytes / (int)sizeof(T);
@@ -197,7 +198,7 @@ __global__ void __launch_bounds__(kSoftLists)
 // d x_j = y_j (g_j - sum_k g_k y_k); y from `ysaved` when given, else
 // recomputed from x (max and normaliser recomputed per list).
 template <class T>
-__global__ void __launch_bounds__(kSoftLists)
+__global__ void __launch_bounds__(kSoftThreads)
     softmax_backward_kernel(T* __restrict__ gx, const T* __restrict__ gy,
                             const T* __restrict__ x, const T* __restrict__ ysaved,
                             const int64_t* __restrict__ offsets, long long nlists) {
@@ -262,7 +263,7 @@ __global__ void __launch_bounds__(kSoftLists)
   GB_EXPORT int awkward_gb300_segment_sum_backward_##SUFFIX(                                    \
       T* grad_x, const T* grad_out, const int64_t* offsets, int64_t nlists, void* stream) {    \
     if (nlists <= 0) return 0;                                                                  \
-    sum_backward_kernel<T><<<soft_tiles(nlists), kSoftLists, 0, (cudaStream_t)stream>>>(         \
+    sum_backward_kernel<T><<<soft_tiles(nlists), kSoftThreads, 0, (cudaStream_t)stream>>>(         \
         grad_x, grad_out, offsets, nlists);                                                     \
     return (int)cudaGetLastError();                                                             \
   }                                                                                             \
@@ -284,7 +285,7 @@ __global__ void __launch_bounds__(kSoftLists)
   GB_EXPORT int awkward_gb300_jagged_softmax_forward_##SUFFIX(                                  \
       T* y, const T* x, const int64_t* offsets, int64_t nlists, void* stream) {                \
     if (nlists <= 0) return 0;                                                                  \
-    softmax_forward_kernel<T><<<soft_tiles(nlists), kSoftLists, 0, (cudaStream_t)stream>>>(      \
+    softmax_forward_kernel<T><<<soft_tiles(nlists), kSoftThreads, 0, (cudaStream_t)stream>>>(      \
         y, x, offsets, nlists);                                                                 \
     return (int)cudaGetLastError();                                                             \
   }                                                                                             \
@@ -292,7 +293,7 @@ __global__ void __launch_bounds__(kSoftLists)
       T* grad_x, const T* grad_y, const T* x, const T* y_saved, const int64_t* offsets,        \
       int64_t nlists, void* stream) {                                                           \
     if (nlists <= 0) return 0;                                                                  \
-    softmax_backward_kernel<T><<<soft_tiles(nlists), kSoftLists, 0, (cudaStream_t)stream>>>(     \
+    softmax_backward_kernel<T><<<soft_tiles(nlists), kSoftThreads, 0, (cudaStream_t)stream>>>(     \
         grad_x, grad_y, x, y_saved, offsets, nlists);                                           \
     return (int)cudaGetLastError();                                                             \
   }
