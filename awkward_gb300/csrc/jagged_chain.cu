@@ -12,10 +12,12 @@
 // offsets.  A tile of at most kMaskBits elements is first staged as a bitmap
 // in shared memory (16-byte loads); the counts are popcounts of it, each
 // thread lists its lists' true positions in rank order in shared memory, and
-// the tile's positions are copied out coalesced.  A larger tile counts from
-// global memory and then each warp walks a contiguous share of its elements
-// 32 at a time, ranking the true entries with a ballot prefix and writing the
-// local index (position within its list) of each at its rank.
+// the tile's positions are copied out coalesced (a tile with more than
+// kMaskPos true entries writes them from the lists' threads directly).  A
+// larger tile counts from global memory and then each warp walks a contiguous
+// share of its elements 32 at a time, ranking the true entries with a ballot
+// prefix and writing the local index (position within its list) of each at
+// its rank.
 #include "list_tile.cuh"
 
 using namespace gb;
@@ -29,12 +31,14 @@ struct MaskTile {
 };
 
 // A tile whose mask bytes (plus the first byte's offset in its 16-byte line)
-// fit kMaskBits is staged as a bitmap in shared memory; its true entries'
-// positions are gathered there in rank order and copied out coalesced.
+// fit kMaskBits is staged as a bitmap in shared memory; the positions of its
+// true entries (when at most kMaskPos) are gathered there in rank order and
+// copied out coalesced, or else written straight to global memory.
 constexpr int kMaskBits = 16384;
+constexpr int kMaskPos = 8192;
 struct MaskStage {
   unsigned bits[kMaskBits / 32];   // bit p: byte (tile's first byte - shift + p) is nonzero
-  unsigned short pos[kMaskBits];   // position within its list of each true entry, by rank
+  unsigned short pos[kMaskPos];    // position within its list of each true entry, by rank
 };
 
 // 4 mask bytes -> 4 bits (byte k nonzero -> bit k).  Bit 7 of each byte of
@@ -61,7 +65,7 @@ __device__ __forceinline__ int bitmap_count(const unsigned* bits, int a, int b) 
   return n;
 }
 
-__global__ void __launch_bounds__(kTileBlock)
+__global__ void __launch_bounds__(kTileBlock, 6)
     mask_to_index_kernel(int64_t* __restrict__ tooffsets, int64_t* __restrict__ toindex,
                          const uint8_t* __restrict__ mask, const int64_t* __restrict__ offsets,
                          long long nlists, long long ntiles, ScanTiles st, uint64_t* err) {
@@ -128,6 +132,8 @@ __global__ void __launch_bounds__(kTileBlock)
   if (staged) {
     // each thread lists its lists' true entries in rank order, then the tile's
     // positions are copied out with consecutive threads on consecutive ranks
+    const int ntrue = (int)sm.total;
+    const bool gather = ntrue <= kMaskPos;
 #pragma unroll
     for (int r = 0; r < kTileLPT; r++) {
       const int li = threadIdx.x * kTileLPT + r;
@@ -141,12 +147,15 @@ __global__ void __launch_bounds__(kTileBlock)
         while (word) {
           const int bit = __ffs(word) - 1;
           word &= word - 1;
-          ms.pos[o++] = (unsigned short)(32 * w + bit - a);
+          const int v = 32 * w + bit - a;
+          if (gather) ms.pos[o] = (unsigned short)v;
+          else toindex[prefix + o] = v;
+          o++;
         }
       }
     }
+    if (!gather) return;
     __syncthreads();
-    const int ntrue = (int)sm.total;
     for (int i = threadIdx.x; i < ntrue; i += kTileBlock) toindex[prefix + i] = ms.pos[i];
     return;
   }
