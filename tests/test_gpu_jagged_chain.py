@@ -132,6 +132,58 @@ def test_index_chain_matches_oracle():
     np.testing.assert_array_equal(content.cpu().numpy(), x[e_carry])
 
 
+@pytest.mark.parametrize("pattern", ["sparse_long", "mixed"])
+def test_apply_and_range_slot_search_branches(pattern):
+    """Tiles of 1024 lists with at least 1.5 output slots per list fill their
+    outputs in warp steps of 32 slots: the lanes' lists come from a popcount of
+    the list ends inside the step, a shuffle search when empty lists share an
+    end, and a per-lane walk when 32 or more lists end inside one step.  A long
+    list followed by 63 empty ones puts 32+ ends in one step; the mixed pattern
+    interleaves all three cases."""
+    import torch
+
+    from awkward_gb300 import jagged
+
+    rng = np.random.default_rng(16)
+    if pattern == "sparse_long":
+        L = np.zeros(64 * 2000, np.int64)
+        L[::64] = rng.integers(100, 300, 2000)
+    else:
+        L = rng.poisson(3, 200_000)
+        L[rng.random(len(L)) < 0.3] = 0
+        runs = rng.integers(0, len(L) - 80, 400)
+        for r0 in runs:
+            L[r0:r0 + 40 + int(rng.integers(0, 40))] = 0
+            L[r0] = int(rng.integers(50, 400))
+    off = np.concatenate([[0], np.cumsum(L)]).astype(np.int64)
+    x = rng.standard_normal(int(off[-1])).astype(np.float32)
+    # every position of every list, as a jagged index: slots = elements
+    ioff = off.copy()
+    idx = np.concatenate([np.arange(l) for l in L if l] or [np.zeros(0, np.int64)]).astype(np.int64)
+    too, content = jagged.getitem_jagged_index(torch.from_numpy(off).cuda(),
+                                               torch.from_numpy(x).cuda(),
+                                               torch.from_numpy(ioff).cuda(),
+                                               torch.from_numpy(idx).cuda())
+    e_too, e_carry = _oracle_apply(off, ioff, idx)
+    np.testing.assert_array_equal(too.cpu().numpy(), e_too)
+    np.testing.assert_array_equal(content.cpu().numpy(), x[e_carry])
+    # [..., 1:] on the same lists
+    nxo, nxc = jagged.inner_range(torch.from_numpy(off).cuda(), 1, None, None)
+    n = len(off) - 1
+    lib = oracle.load()
+    cl = np.zeros(1, np.int64)
+    assert oracle.call(lib, "awkward_ListArray64_getitem_next_range_carrylength", carrylength=cl,
+                       fromstarts=off[:-1].copy(), fromstops=off[1:].copy(), lenstarts=n,
+                       start=1, stop=jagged.SLICE_NONE, step=1)[0] is None
+    e_off = np.zeros(n + 1, np.int64)
+    e_carry2 = np.zeros(max(int(cl[0]), 1), np.int64)
+    assert oracle.call(lib, "awkward_ListArray64_getitem_next_range_64", tooffsets=e_off,
+                       tocarry=e_carry2, fromstarts=off[:-1].copy(), fromstops=off[1:].copy(),
+                       lenstarts=n, start=1, stop=jagged.SLICE_NONE, step=1)[0] is None
+    np.testing.assert_array_equal(nxo.cpu().numpy(), e_off)
+    np.testing.assert_array_equal(nxc.cpu().numpy(), e_carry2[: int(cl[0])])
+
+
 def test_index_chain_error_is_awkwards():
     import torch
 
