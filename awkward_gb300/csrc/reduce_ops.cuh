@@ -58,7 +58,7 @@ __device__ __forceinline__ bool num_better(T b, T a) {
   }
 }
 
-// ---------------------------------------------------------------- exact sum
+// ---------------------------------------------------------------- fixed-point sum
 // Fixed-point accumulator for float64 sums on the integer pipe: the value is
 // acc * 2^(anchor - 1075); every addend's 53-bit significand is aligned to the
 // anchor (the largest exponent seen; bits below the anchor's unit are
