@@ -71,7 +71,8 @@ def cfunc(name):
     return f
 
 
-_EXT_CTYPES = {"int64_t": ctypes.c_int64, "uint64_t": ctypes.c_uint64, "int32_t": ctypes.c_int32}
+_EXT_CTYPES = {"int64_t": ctypes.c_int64, "uint64_t": ctypes.c_uint64, "int32_t": ctypes.c_int32,
+               "uint32_t": ctypes.c_uint32}
 
 
 def ext_cfunc(name):

@@ -18,9 +18,9 @@ library (held on every GPU that loads it until exit) instead of a
 pool allocation.  sliceouterlen above AWKWARD_GB300_NOALLOC_MAX_LISTS
 returns cudaErrorInvalidValue (1) and launches nothing.  All calls
 share the array: calls that overlap on the GPU (other streams or
-threads) race and must be ordered by the caller.  The first call on
-each device looks up the array's device address, so make it before
-any stream capture on that device."""
+threads) race and must be ordered by the caller.  The first call in
+each CUDA context looks up the array's device address (cached per
+device and context), so make it before any stream capture there."""
 
 _AUTOGRAD_COMMENT = """backward kernels of differentiable jagged operations (torch.autograd
 in awkward_gb300/autograd.py).  No counterpart in awkward, which has no
@@ -115,16 +115,29 @@ EXTENSIONS["awkward_gb300_reduce_sum_max_argmax_host_float64"] = (
      ("double*", "d_x"), ("int64_t*", "d_offsets"), ("double*", "d_sum"), ("double*", "d_max"),
      ("int64_t*", "d_argmax"), ("int64_t", "chunks"), ("void*", "stream")], "pipeline")
 
+_SELFTEST_COMMENT = """self-test of the failure report (no counterpart in awkward): one warp
+runs the decoupled look-back of the scan kernels on tile 1 of a fresh
+scan whose tile 0 never publishes, with a spin limit of `spin_limit`
+polls (clamped to 1..2^22; each poll sleeps at most 256 ns).  The wait
+runs out and the kernel sets err_code to invocation_index*256 + 32, the
+library's "bounded wait gave up" code, then returns; the GPU stays
+usable.  It is how the tests check that a stalled look-back ends with an
+error the host can read instead of a hang."""
+
+EXTENSIONS["awkward_gb300_selftest_lookback_timeout"] = (
+    [("uint32_t", "spin_limit"), ("uint64_t", "invocation_index"), ("uint64_t*", "err_code"),
+     ("void*", "stream")], "selftest")
+
 GROUP_COMMENTS = {"noalloc": _NOALLOC_COMMENT, "autograd": _AUTOGRAD_COMMENT,
                   "jagged": _JAGGED_COMMENT, "batch": _BATCH_COMMENT,
-                  "pipeline": _PIPELINE_COMMENT}
+                  "pipeline": _PIPELINE_COMMENT, "selftest": _SELFTEST_COMMENT}
 GROUP_DEFINES = {"noalloc": ["#define AWKWARD_GB300_NOALLOC_MAX_LISTS 67108864LL"]}
 
 
 def header_lines():
     """Declarations of the extension entry points, grouped, for the C header."""
     out = []
-    for group in ("noalloc", "jagged", "autograd", "batch", "pipeline"):
+    for group in ("noalloc", "jagged", "autograd", "batch", "pipeline", "selftest"):
         out.append("")
         text = GROUP_COMMENTS[group].splitlines()
         out.append(f"/* ---- {text[0]}")

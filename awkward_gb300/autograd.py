@@ -7,7 +7,8 @@ are indexed globally).  Every forward and backward pass runs this library's
 CUDA kernels; there is no fallback.
 
 * ``segment_sum(values, offsets)``   -> per-list sums (float32 accumulates in
-  float32 in list order, float64 exactly rounded); backward broadcasts the
+  float32 in list order, float64 as a fixed-point sum rounded once, within
+  n*eps*sum|x| of the exact sum); backward broadcasts the
   output gradient to every element of its list.
 * ``segment_max(values, offsets)``   -> per-list maxima (``-inf`` for an empty
   list; NaN ignored, as ak.max); backward routes each list's gradient to the

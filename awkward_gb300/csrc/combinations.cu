@@ -164,9 +164,10 @@ __global__ void __launch_bounds__(kTileBlock)
   // from the list of the step's first slot (warp_step_lists).
   constexpr int kWarps = kTileBlock / 32;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  if ((n == 2 || n == 3) && total < (1ll << 31)) {
-    // pairs or triples of a tile with fewer than 2^31 of them: tile-local
-    // positions in 32 bits
+  if ((n == 2 || n == 3) && total < (1ll << 31) - 64) {
+    // pairs or triples of a tile with fewer than 2^31 - 64 of them: tile-local
+    // positions in 32 bits (the step positions g + 32 and g + lane stay
+    // below 2^31)
     __shared__ int loc32[kTileLists + 1];
     for (int i = threadIdx.x; i <= kTileLists; i += kTileBlock) loc32[i] = (int)sm.loc[i];
     __syncthreads();

@@ -196,7 +196,8 @@ __device__ __forceinline__ unsigned long long lb_load(const unsigned long long* 
 // and error `timeout_code` is raised, so the kernel always terminates.
 __device__ __forceinline__ long long lookback_exclusive(const ScanTiles& st, long long tile,
                                                         long long aggregate, uint64_t inv,
-                                                        uint64_t* err, int timeout_code) {
+                                                        uint64_t* err, int timeout_code,
+                                                        uint32_t spin_limit = kSpinLimit) {
   const int lane = threadIdx.x & 31;
   if (tile == 0) {
     if (lane == 0) lb_publish(st.status, 2, (unsigned long long)aggregate);
@@ -214,7 +215,7 @@ __device__ __forceinline__ long long lookback_exclusive(const ScanTiles& st, lon
       uint32_t ns = 32;
       word = lb_load(st.status + p);
       while ((word >> 62) == 0) {
-        if (++it > kSpinLimit) { timed_out = true; word = 2ull << 62; break; }
+        if (++it > spin_limit) { timed_out = true; word = 2ull << 62; break; }
         __nanosleep(ns);
         if (ns < 256) ns <<= 1;
         word = lb_load(st.status + p);

@@ -11,6 +11,8 @@
 //
 // Error codes are the indices of the messages in awkward's CUDA kernels of
 // the same name (their `// message:` enum order).
+#include <dlfcn.h>
+
 #include <mutex>
 
 #include "list_tile.cuh"
@@ -547,10 +549,12 @@ GB_LOCALINDEX(awkward_ListArray64_localindex_64, int64_t)
 //     offsets: issue them on one stream or order them with events.
 // The array's host-side name is only a stand-in symbol, not a device
 // address, so the device address is looked up with cudaGetSymbolAddress the
-// first time the entry point runs on each device (with that device current)
-// and cached.  That first call per device should therefore come before any
-// stream capture on that device.  The entry point calls no cudaMalloc,
-// cudaFree or other allocating routine.
+// first time the entry point runs in a context (with that context's device
+// current) and cached per (device, CUDA context): a context made later on the
+// same device, for instance after cudaDeviceReset, gets its own lookup.  The
+// first call in a context should therefore come before any stream capture
+// on it.  The entry point calls no cudaMalloc, cudaFree or other allocating
+// routine.
 namespace {
 
 constexpr long long kNoAllocMaxTiles = 1ll << 16;
@@ -559,25 +563,54 @@ constexpr long long kNoAllocTileWords = kNoAllocMaxTiles + 1;  // + the ticket c
 
 static __device__ __align__(256) unsigned long long g_noalloc_tiles[kNoAllocTileWords];
 
-constexpr int kNoAllocMaxDevices = 64;
+struct NoAllocEntry {
+  int dev;
+  void* ctx;
+  unsigned long long* addr;
+};
+constexpr int kNoAllocCache = 64;
 std::mutex g_noalloc_mutex;
-unsigned long long* g_noalloc_addr[kNoAllocMaxDevices] = {};
+NoAllocEntry g_noalloc_cache[kNoAllocCache];
+int g_noalloc_used = 0;
 
-// Device address of g_noalloc_tiles on the current device (looked up once).
+// The current CUDA context (the driver's cuCtxGetCurrent, found in the driver
+// library the runtime has already loaded), or null if it cannot be asked.
+void* current_context() {
+  using Fn = int (*)(void**);
+  static Fn fn = [] {
+    void* h = dlopen("libcuda.so.1", RTLD_NOW | RTLD_NOLOAD);
+    if (!h) h = dlopen("libcuda.so.1", RTLD_NOW);
+    return h ? reinterpret_cast<Fn>(dlsym(h, "cuCtxGetCurrent")) : nullptr;
+  }();
+  void* ctx = nullptr;
+  if (!fn || fn(&ctx) != 0) return nullptr;
+  return ctx;
+}
+
+// Device address of g_noalloc_tiles in the current context (looked up once
+// per device and context).
 cudaError_t noalloc_tiles_address(unsigned long long** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
-  if (dev < 0 || dev >= kNoAllocMaxDevices) return cudaErrorInvalidDevice;
+  void* ctx = current_context();
   std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_addr[dev]) {
-    void* ptr = nullptr;
-    e = cudaGetSymbolAddress(&ptr, g_noalloc_tiles);
-    if (e != cudaSuccess) return e;
-    if (!ptr) return cudaErrorInvalidSymbol;
-    g_noalloc_addr[dev] = static_cast<unsigned long long*>(ptr);
-  }
-  *out = g_noalloc_addr[dev];
+  if (ctx)
+    for (int i = 0; i < g_noalloc_used; i++)
+      if (g_noalloc_cache[i].dev == dev && g_noalloc_cache[i].ctx == ctx) {
+        *out = g_noalloc_cache[i].addr;
+        return cudaSuccess;
+      }
+  // (the lookup also makes the device's runtime context current when no
+  // context was current yet)
+  void* ptr = nullptr;
+  e = cudaGetSymbolAddress(&ptr, g_noalloc_tiles);
+  if (e != cudaSuccess) return e;
+  if (!ptr) return cudaErrorInvalidSymbol;
+  if (!ctx) ctx = current_context();
+  if (ctx && g_noalloc_used < kNoAllocCache)
+    g_noalloc_cache[g_noalloc_used++] = {dev, ctx, static_cast<unsigned long long*>(ptr)};
+  *out = static_cast<unsigned long long*>(ptr);
   return cudaSuccess;
 }
 

@@ -19,9 +19,18 @@ path, for callers holding torch CUDA tensors (the cupy adapter in
 Arguments: List[T] -> a contiguous CUDA tensor of dtype T (bool as
 torch.bool); List[List[T]] -> a sequence of such tensors; scalars -> Python
 numbers.
+
+Fault injection (host side, for testing callers' error handling): with
+``AWKWARD_GB300_FAULT="<specialization or family>:<code>"`` every call of a
+matching kernel still launches, and then the stream's error word records
+``invocation_index * 256 + code`` exactly as a failing kernel would, so the
+next ``synchronize()`` raises that code's message (code 32: the library's
+"bounded wait gave up").  No kernel is made to fail on the GPU.
 """
 
 from __future__ import annotations
+
+import os
 
 import numpy as np
 import torch
@@ -53,6 +62,26 @@ def kernel_key(name):
     return (rec["family"],) + tuple(NP_OF_C[a[1]] for a in rec["args"] if a[3] > 0)
 
 
+FAULT_ENV = "AWKWARD_GB300_FAULT"
+
+
+def injected_fault(name, family, env=None):
+    """The error code AWKWARD_GB300_FAULT forces on kernel ``name``, or None.
+
+    The variable holds ``<specialization or family>:<code>`` with code in
+    0..255; anything else is ignored.
+    """
+    spec = (os.environ if env is None else env).get(FAULT_ENV, "")
+    target, sep, code = spec.rpartition(":")
+    if not sep or target not in (name, family):
+        return None
+    try:
+        c = int(code)
+    except ValueError:
+        return None
+    return c if 0 <= c < (1 << ERROR_BITS) else None
+
+
 class _Invocation:
     __slots__ = ("name", "keepalive")
 
@@ -67,6 +96,13 @@ class _StreamContext:
     def __init__(self, device):
         self.err = torch.full((1,), -1, dtype=torch.int64, device=device)  # NO_ERROR
         self.pending = []
+
+    def record_error(self, invocation, code, stream):
+        """Lower the error word to invocation*256 + code on `stream` (as atomicMin does)."""
+        word = invocation * (1 << ERROR_BITS) + code
+        with torch.cuda.stream(stream):
+            w = torch.full_like(self.err, word)
+            self.err.copy_(torch.where((self.err < 0) | (self.err > w), w, self.err))
 
 
 class GB300Kernel:
@@ -131,6 +167,9 @@ class GB300Kernel:
         rc = self._f(*cargs, invocation, ctx.err.data_ptr(), stream.cuda_stream)
         if rc != 0:
             raise RuntimeError(f"{self.name}: CUDA launch failed with cudaError {rc}")
+        code = injected_fault(self.name, self.family)
+        if code is not None:
+            ctx.record_error(invocation, code, stream)
 
 
 class GB300Backend:
@@ -170,6 +209,20 @@ class GB300Backend:
         if ctx is None:
             ctx = self._contexts[key] = _StreamContext(stream.device)
         return ctx
+
+    def selftest_lookback_timeout(self, spin_limit=1000):
+        """Launch the look-back self-test (awkward_gb300_selftest_lookback_timeout)
+        on the current stream as one more invocation: its wait on a tile that
+        never publishes runs out after `spin_limit` polls, so the next
+        synchronize() raises the "bounded wait gave up" ValueError."""
+        stream = torch.cuda.current_stream()
+        ctx = self._context(stream)
+        invocation = len(ctx.pending)
+        ctx.pending.append(_Invocation("awkward_gb300_selftest_lookback_timeout", []))
+        rc = _abi.ext_cfunc("awkward_gb300_selftest_lookback_timeout")(
+            int(spin_limit), invocation, ctx.err.data_ptr(), stream.cuda_stream)
+        if rc != 0:
+            raise RuntimeError(f"look-back self-test: CUDA launch failed with cudaError {rc}")
 
     def synchronize(self, stream=None):
         """Wait for the stream; raise ValueError for the first failed invocation."""

@@ -44,15 +44,23 @@ def local_shard(offsets, content, rank, world):
 
 
 def exclusive_prefix_of_totals(total, group=None):
-    """Sum of the totals of all lower ranks (allgather of one int64)."""
+    """Sum of the totals of all lower ranks (allgather of one int64).
+
+    The exchanged tensor lives where the group's backend wants it: on the
+    rank's current CUDA device for NCCL (which takes no host tensors), in host
+    memory for gloo.
+    """
     import torch
     import torch.distributed as dist
 
     if not dist.is_available() or not dist.is_initialized():
         return 0
-    t = torch.tensor([int(total)], dtype=torch.int64)
+    dev = torch.device("cpu")
+    if dist.get_backend(group) == "nccl":
+        dev = torch.device("cuda", torch.cuda.current_device())
+    t = torch.tensor([int(total)], dtype=torch.int64, device=dev)
     world = dist.get_world_size(group)
-    parts = [torch.zeros(1, dtype=torch.int64) for _ in range(world)]
+    parts = [torch.zeros(1, dtype=torch.int64, device=dev) for _ in range(world)]
     dist.all_gather(parts, t, group=group)
     rank = dist.get_rank(group)
     return int(sum(int(p.item()) for p in parts[:rank]))

@@ -182,16 +182,12 @@ def cpu_reduce_step(lib_kind, off, x, outs, threads):
 
     n = len(off) - 1
     oracle.parallel_reduce("awkward_reduce_sum_float64_float64_64", outs[0], x, off, n, threads)
-    oracle.parallel_reduce("awkward_reduce_max_float64_float64_64", outs[1], x, off, n, threads)
+    oracle.parallel_reduce("awkward_reduce_max_float64_float64_64", outs[1], x, off, n, threads,
+                           identity=-np.inf)
     oracle.parallel_reduce("awkward_reduce_argmax_float64_64", outs[2], x, off, n, threads)
 
 
-def cpu_baseline(n_lists, seed, target_s=10.0):
-    """The C restatement of awkward-cpp's reducers on all host cores, bounded sample."""
-    import oracle
-
-    threads = os.cpu_count() or 1
-    off, x = make_c1(n_lists, seed)
+def _time_cpu_steps(off, x, threads, target_s):
     n = len(off) - 1
     outs = [np.empty(n), np.empty(n), np.empty(n, np.int64)]
     cpu_reduce_step("port", off, x, outs, threads)  # warm
@@ -202,11 +198,54 @@ def cpu_baseline(n_lists, seed, target_s=10.0):
         reps += 1
         if time.perf_counter() - t0 > target_s:
             break
-    dt = (time.perf_counter() - t0) / reps
-    gbs = 3 * algorithmic_bytes(n, len(x)) / dt / 1e9
-    return {"value": round(gbs, 3), "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} C1 lists (Poisson(8), float64), sum+max+argmax, {reps} reps, "
-                      f"{dt*1e3:.1f} ms/step", "ms_per_step": dt * 1e3}
+    return (time.perf_counter() - t0) / reps, reps
+
+
+def cpu_baseline(off, x, target_s=6.0):
+    """The C restatement of awkward-cpp's reducers on the full workload:
+    on all host cores (pthreads over list ranges), and on one core (awkward-cpp
+    itself is single-threaded: its CMakeLists.txt builds the CPU kernels with
+    no threading)."""
+    threads = os.cpu_count() or 1
+    n = len(off) - 1
+    nbytes = 3 * algorithmic_bytes(n, len(x))
+    dt, reps = _time_cpu_steps(off, x, threads, target_s)
+    dt1, reps1 = _time_cpu_steps(off, x, 1, target_s)
+    return {"value": round(nbytes / dt / 1e9, 3), "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"full workload: {n} C1 lists (Poisson(8), float64), sum+max+argmax, "
+                      f"{reps} steps of {dt*1e3:.1f} ms; awkward-cpp restated in oracle/",
+            "single_core": {"value": round(nbytes / dt1 / 1e9, 3), "unit": UNIT, "cores": 1,
+                            "ms_per_step": round(dt1 * 1e3, 2), "steps": reps1},
+            "ms_per_step": round(dt * 1e3, 2)}
+
+
+def c1_config(n, e, world):
+    """The `config` object of both arms (same keys and values for one workload)."""
+    return {"workload": f"C1 reducers @ {n} lists Poisson(8) float64 (sum+max+argmax)",
+            "lists_per_gpu": n, "elements_per_gpu": e,
+            "l2": f"inputs {(8 * e + 8 * (n + 1)) / 1e6:.0f} MB vs 129 MB L2: "
+                  + ("larger, no flush needed" if 8 * e + 8 * (n + 1) > 129e6
+                     else "SMALLER: timings include L2 reuse"),
+            "parallelism": f"{world} independent shard(s), no collective"}
+
+
+def c1_parity(off, x, got_sum, got_max, got_arg):
+    """The timed outputs against the oracle on the full input: argmax and max
+    bit for bit (C restatement over all host cores), the float sum's error
+    figures against the FP64 compensated-sum oracle (bound 4*n*eps*sum|x|)."""
+    import oracle
+
+    threads = os.cpu_count() or 1
+    n = len(off) - 1
+    e_max, e_arg = np.empty(n), np.empty(n, np.int64)
+    oracle.parallel_reduce("awkward_reduce_max_float64_float64_64", e_max, x, off, n, threads,
+                           identity=-np.inf)
+    oracle.parallel_reduce("awkward_reduce_argmax_float64_64", e_arg, x, off, n, threads)
+    rep = oracle.sum_error_report(got_sum, x, off, nthreads=threads)
+    return {"argmax_bit_exact": bool(np.array_equal(got_arg, e_arg)),
+            "max_bit_exact": bool(np.array_equal(got_max.view(np.int64), e_max.view(np.int64))),
+            "sum_err": {k: (float(f"{v:.4g}") if isinstance(v, float) else v) for k, v in rep.items()},
+            "sum_bound": "|gpu - compensated| <= 4*n*eps*sum|x| per list; ratio = err/(n*eps*sum|x|)"}
 
 
 def run_reference(args):
@@ -230,8 +269,7 @@ def run_reference(args):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(dt * 1e3, 3), "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded C1 generator)",
-            "config": {"workload": f"C1 reducers @ {n} lists Poisson(8) float64",
-                       "lists": n, "elements": int(len(x))},
+            "config": c1_config(n, int(len(x)), int(os.environ.get("WORLD_SIZE", "1"))),
             "cpu_baseline": {"value": round(gbs, 3), "unit": UNIT, "cores": threads,
                              "kind": "port",
                              "sample": f"full workload ({n} lists) per step, pthreads over "
@@ -685,6 +723,7 @@ def run_gb300(args):
                 torch.empty(n, dtype=torch.float64).pin_memory(),
                 torch.empty(n, dtype=torch.int64).pin_memory())
     ws = pipeline.Workspace(n, int(off_h[-1]), device=dev)
+    dev_outs = (o_sum.cpu().numpy(), o_max.cpu().numpy(), o_arg.cpu().numpy())
     del x, off, starts  # the workspace holds the device copies
 
     def e2e_step():
@@ -703,6 +742,8 @@ def run_gb300(args):
     torch.cuda.synchronize()
     be.synchronize()
     ms_e2e = reduce_max(s2.elapsed_time(t2) / args.steps)
+    e2e_same = all(np.array_equal(a.numpy().view(np.int64), b.view(np.int64))
+                   for a, b in zip(outs_pin, dev_outs))
     e2e_value = world * step_bytes / (ms_e2e * 1e-3) / 1e9
 
     dominant = max(per, key=per.get)
@@ -714,12 +755,7 @@ def run_gb300(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded C1 generator: Poisson(8) lengths, 1% empty, N(0,1))",
-        "config": {"workload": f"C1 reducers @ {n} lists Poisson(8) float64 (sum+max+argmax)",
-                   "lists_per_gpu": n, "elements_per_gpu": e,
-                   "l2": f"inputs {(8 * e + 8 * (n + 1)) / 1e6:.0f} MB vs 129 MB L2: "
-                         + ("larger, no flush needed" if 8 * e + 8 * (n + 1) > 129e6
-                            else "SMALLER: timings include L2 reuse"),
-                   "parallelism": f"{world} independent shard(s), no collective"},
+        "config": c1_config(n, e, world),
         "per_kernel_ms": {k: round(v, 4) for k, v in per.items()},
         "roofline": {"bound": "hbm", "kernel": f"seg_reduce ({dominant})",
                      "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -729,7 +765,8 @@ def run_gb300(args):
         "e2e": {"value": round(e2e_value, 2), "unit": UNIT,
                 "h2d_bytes_per_step": int(8 * e + 8 * (n + 1)),
                 "d2h_bytes_per_step": int(3 * 8 * n), "ms_per_step": round(ms_e2e, 4),
-                "path": f"awkward_gb300.pipeline.reduce_host, {args.chunks} chunks"},
+                "path": f"awkward_gb300.pipeline.reduce_host, {args.chunks} chunks",
+                "outputs_equal_device_path": e2e_same},
         "gpu_launches": args.steps * 3 * 2,
         "clocks": sampler.summary(),
     }
@@ -741,8 +778,8 @@ def run_gb300(args):
         line["sort"] = measure_sort(be, dev, max(args.steps // 2, 5), args.warmup)
         line["nonlocal_reduce"] = measure_nonlocal(be, dev, max(args.steps // 2, 5), args.warmup)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = {k: v for k, v in cpu_baseline(2_000_000, 1, 8.0).items()
-                                if k != "ms_per_step"}
+        line["parity"] = c1_parity(off_h, x_h, *dev_outs)
+        line["cpu_baseline"] = cpu_baseline(off_h, x_h)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

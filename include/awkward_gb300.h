@@ -719,9 +719,9 @@ int awkward_sort_float64(double* toptr, const double* fromptr, int64_t length, c
  * pool allocation.  sliceouterlen above AWKWARD_GB300_NOALLOC_MAX_LISTS
  * returns cudaErrorInvalidValue (1) and launches nothing.  All calls
  * share the array: calls that overlap on the GPU (other streams or
- * threads) race and must be ordered by the caller.  The first call on
- * each device looks up the array's device address, so make it before
- * any stream capture on that device. */
+ * threads) race and must be ordered by the caller.  The first call in
+ * each CUDA context looks up the array's device address (cached per
+ * device and context), so make it before any stream capture there. */
 #define AWKWARD_GB300_NOALLOC_MAX_LISTS 67108864LL
 int awkward_ListArray64_getitem_jagged_apply_64_noalloc(int64_t* tooffsets, int64_t* tocarry, const int64_t* slicestarts, const int64_t* slicestops, int64_t sliceouterlen, const int64_t* sliceindex, int64_t sliceinnerlen, const int64_t* fromstarts, const int64_t* fromstops, int64_t contentlen, uint64_t invocation_index, uint64_t* err_code, void* stream);
 
@@ -779,6 +779,16 @@ int awkward_gb300_batch_plan_destroy(void* plan);
  * (element j at d_x[j]), d_offsets [nlists + 1], three outputs [nlists].
  * Returns after enqueueing; `stream` waits for the last copy back. */
 int awkward_gb300_reduce_sum_max_argmax_host_float64(double* h_sum, double* h_max, int64_t* h_argmax, const double* h_x, const int64_t* h_offsets, int64_t nlists, double* d_x, int64_t* d_offsets, double* d_sum, double* d_max, int64_t* d_argmax, int64_t chunks, void* stream);
+
+/* ---- self-test of the failure report (no counterpart in awkward): one warp
+ * runs the decoupled look-back of the scan kernels on tile 1 of a fresh
+ * scan whose tile 0 never publishes, with a spin limit of `spin_limit`
+ * polls (clamped to 1..2^22; each poll sleeps at most 256 ns).  The wait
+ * runs out and the kernel sets err_code to invocation_index*256 + 32, the
+ * library's "bounded wait gave up" code, then returns; the GPU stays
+ * usable.  It is how the tests check that a stalled look-back ends with an
+ * error the host can read instead of a hang. */
+int awkward_gb300_selftest_lookback_timeout(uint32_t spin_limit, uint64_t invocation_index, uint64_t* err_code, void* stream);
 
 #ifdef __cplusplus
 }

@@ -1315,6 +1315,45 @@ ORACLE_JAGGED_PROJECT(awkward_MaskedArrayU32_getitem_next_jagged_project, uint32
 ORACLE_JAGGED_PROJECT(awkward_MaskedArray64_getitem_next_jagged_project, int64_t)
 
 /* ======================================================================
+ * FP64 compensated per-list sums: the accuracy reference for float sums.
+ * awkward-cpp's sum (awkward_reduce_sum.cpp:17-23) adds left to right and
+ * rounds after every addition, so it carries up to (n-1)*u*sum|x| of error
+ * (u = 2^-53); the GPU sums in a different order.  Both are judged against
+ * this double-double accumulation instead: every addition is made
+ * error-free with Knuth's TwoSum (s + x = s' + e exactly, in round-to-
+ * nearest double arithmetic, no fused operations) and the errors are
+ * accumulated in a second double, so the result is within u*|S| +
+ * n*u^2*sum|x| of the exact sum S.  Lists holding an infinity or a NaN take
+ * the plain left-to-right sum (IEEE: inf + -inf = NaN).
+ *
+ * out[2b] = the compensated sum of list b, out[2b+1] = sum|x| over it (the
+ * scale of the error bound).  The signature matches the reducers above, so
+ * oracle_parallel_reduce can split it over threads (output size 16 bytes).
+ * ====================================================================== */
+#define ORACLE_SUM_COMPENSATED(NAME, IN)                                       \
+  struct Error NAME(double* out, const IN* fromptr, const int64_t* offsets,    \
+                    int64_t outlength) {                                       \
+    for (int64_t b = 0; b < outlength; b++) {                                  \
+      double s = 0.0, c = 0.0, plain = 0.0, a = 0.0;                           \
+      for (int64_t i = offsets[b]; i < offsets[b + 1]; i++) {                  \
+        const double x = (double)fromptr[i];                                   \
+        const double t = s + x;                                                \
+        const double bp = t - s;                                               \
+        const double e = (s - (t - bp)) + (x - bp);                            \
+        s = t;                                                                 \
+        c += e;                                                                \
+        plain += x;                                                            \
+        a += fabs(x);                                                          \
+      }                                                                        \
+      out[2 * b] = isfinite(plain) ? s + c : plain;                            \
+      out[2 * b + 1] = a;                                                      \
+    }                                                                          \
+    return success();                                                          \
+  }
+ORACLE_SUM_COMPENSATED(oracle_sum_compensated_float64, double)
+ORACLE_SUM_COMPENSATED(oracle_sum_compensated_float32, float)
+
+/* ======================================================================
  * Multi-core runner for the CPU baseline: run one reducer (any of the
  * (toptr, fromptr, offsets, outlength) family above, or argmax/argmin with
  * `starts`) over `nthreads` contiguous list ranges.  Each thread calls the
@@ -1322,10 +1361,13 @@ ORACLE_JAGGED_PROJECT(awkward_MaskedArray64_getitem_next_jagged_project, int64_t
  * ====================================================================== */
 typedef struct Error (*oracle_reduce4_fn)(void*, const void*, const int64_t*, int64_t);
 typedef struct Error (*oracle_reduce5_fn)(void*, const void*, const int64_t*, const int64_t*, int64_t);
+typedef struct Error (*oracle_reduce_ident_fn)(void*, const void*, const int64_t*, int64_t, double);
 
 typedef struct {
   void* fn;
-  int kind; /* 4 = (to, from, offsets, n); 5 = argmax form (to, from, offsets, starts, n) */
+  int kind; /* 4 = (to, from, offsets, n); 5 = argmax form (to, from, offsets, starts, n);
+               6 = float64 max/min form (to, from, offsets, n, identity) */
+  double identity;
   char* toptr;
   const void* fromptr;
   const int64_t* offsets;
@@ -1338,14 +1380,27 @@ static void* oracle_job_run(void* p) {
   if (j->kind == 4)
     ((oracle_reduce4_fn)j->fn)(j->toptr + j->lo * j->outsize, j->fromptr, j->offsets + j->lo,
                                j->hi - j->lo);
+  else if (j->kind == 6)
+    ((oracle_reduce_ident_fn)j->fn)(j->toptr + j->lo * j->outsize, j->fromptr, j->offsets + j->lo,
+                                    j->hi - j->lo, j->identity);
   else
     ((oracle_reduce5_fn)j->fn)(j->toptr + j->lo * j->outsize, j->fromptr, j->offsets + j->lo,
                                NULL, j->hi - j->lo);
   return NULL;
 }
 
+int oracle_parallel_reduce_ident(void* fn, int kind, void* toptr, size_t outsize,
+                                 const void* fromptr, const int64_t* offsets, int64_t outlength,
+                                 int nthreads, double identity);
 int oracle_parallel_reduce(void* fn, int kind, void* toptr, size_t outsize, const void* fromptr,
                            const int64_t* offsets, int64_t outlength, int nthreads) {
+  return oracle_parallel_reduce_ident(fn, kind, toptr, outsize, fromptr, offsets, outlength,
+                                      nthreads, 0.0);
+}
+
+int oracle_parallel_reduce_ident(void* fn, int kind, void* toptr, size_t outsize,
+                                 const void* fromptr, const int64_t* offsets, int64_t outlength,
+                                 int nthreads, double identity) {
   if (nthreads < 1) nthreads = 1;
   if (nthreads > 256) nthreads = 256;
   pthread_t th[256];
@@ -1359,6 +1414,7 @@ int oracle_parallel_reduce(void* fn, int kind, void* toptr, size_t outsize, cons
     jobs[t].lo = outlength * t / nthreads;
     jobs[t].hi = outlength * (t + 1) / nthreads;
     jobs[t].outsize = outsize;
+    jobs[t].identity = identity;
     if (pthread_create(&th[t], NULL, oracle_job_run, &jobs[t]) != 0) return -1;
   }
   for (int t = 0; t < nthreads; t++) pthread_join(th[t], NULL);

@@ -40,7 +40,12 @@ def test_reference_arm_prints_one_contract_line():
         assert k in d, k
     assert d["steps"] == 2 and d["warmup"] == 1 and d["n_gpus"] == 1
     assert d["value"] > 0 and d["higher_is_better"] is True
-    assert d["config"]["lists"] == 50000 and "workload" in d["config"]
+    assert d["config"]["lists_per_gpu"] == 50000 and "workload" in d["config"]
+    # the GPU arm builds its config with the same function (same keys, same workload)
+    sys.path.insert(0, ROOT)
+    import bench
+
+    assert d["config"] == bench.c1_config(50000, d["config"]["elements_per_gpu"], 1)
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
     e2e = d["e2e"]

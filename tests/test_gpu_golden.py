@@ -1,10 +1,12 @@
 """GPU parity: every entry point against awkward's golden vectors and awkward-cpp's outputs.
 
 Integer, index, boolean, count, offsets, carry and combinations outputs and
-max/min values must be bit-identical.  Order-dependent floating-point sums
-(sum, prod, sum of squares/powers, centered sum of squares) must be within
-4*n*eps*sum|term| of awkward-cpp's left-to-right result, per list (n = list
-length, eps of the output type); non-finite results must match exactly.
+max/min values must be bit-identical.  Float sums (awkward_reduce_sum with a
+float output) must be within 4*n*eps*sum|x| of the FP64 compensated-sum
+oracle, per list (n = list length, eps of the output type).  The other
+order-dependent floating-point reductions (prod, sum of squares/powers,
+centered sum of squares) must be within 4*n*eps*sum|term| of awkward-cpp's
+left-to-right result.  Non-finite results must match exactly.
 """
 
 import math
@@ -60,6 +62,15 @@ def check_float_sum_like(name, kw, got, exp):
         n = np.diff(off).astype(np.float64)[: len(exp)]
         tiny = np.finfo(np.float32 if out_t == "float" else np.float64).tiny
         bound = 4 * np.maximum(n, 1) * eps * np.abs(exp) + 64 * tiny
+    elif fam == "awkward_reduce_sum":
+        import oracle
+
+        x = np.asarray(kw["fromptr"])
+        x = x if x.dtype in (np.float32, np.float64) else x.astype(np.float64)
+        m = len(exp)
+        rep = oracle.sum_error_report(got, x, off[: m + 1], eps=float(eps))
+        assert rep["nonfinite_ok"] and rep["within"], (name, rep)
+        return
     else:
         with np.errstate(all="ignore"):
             t = _terms(name, kw)

@@ -12,8 +12,11 @@ that its outputs equal those of the pool-based entry point
 ``awkward_ListArray64_getitem_jagged_apply_64`` on the same inputs, bit for bit
 (integer offsets and carries), on two calls in a row: the second call is
 smaller than the first, so tile states left in the shared array by the first
-call would corrupt its offsets if the entry point did not clear them.  A call
-above the stated maximum must be refused without launching anything.
+call would corrupt its offsets if the entry point did not clear them.  The
+same outputs are checked against the CPU oracle (the C restatement of
+awkward-cpp's kernel), an index out of range must raise awkward's error
+through the same error word as the pooled entry point, and a call above the
+stated maximum must be refused without launching anything.
 
 The file name puts it last in collection order; it needs no state from other
 tests and also passes alone in a fresh process.
@@ -102,3 +105,45 @@ def test_noalloc_refuses_sizes_above_its_maximum():
     # refused on the host before any pointer is touched or anything launched
     rc = fn(None, None, None, None, MAX_LISTS + 1, None, 0, None, None, 0, 0, None, None)
     assert rc == CUDA_ERROR_INVALID_VALUE
+
+
+def _oracle(off, soff, idx):
+    import oracle
+
+    n = len(off) - 1
+    to_off = np.zeros(n + 1, np.int64)
+    to_carry = np.zeros(max(len(idx), 1), np.int64)
+    msg, _ident, _att = oracle.call(
+        oracle.load(), POOLED, tooffsets=to_off, tocarry=to_carry,
+        slicestarts=np.ascontiguousarray(soff[:-1]), slicestops=np.ascontiguousarray(soff[1:]),
+        sliceouterlen=n, sliceindex=np.ascontiguousarray(idx), sliceinnerlen=len(idx),
+        fromstarts=np.ascontiguousarray(off[:-1]), fromstops=np.ascontiguousarray(off[1:]),
+        contentlen=int(off[-1]))
+    return msg, to_off, to_carry[: len(idx)]
+
+
+def test_noalloc_matches_the_oracle():
+    fn = _noalloc_fn()
+    off, soff, idx = _case(30_000, 13)
+    rc, err, got_off, got_carry = _run(fn, off, soff, idx)
+    msg, exp_off, exp_carry = _oracle(off, soff, idx)
+    assert rc == 0 and err == NO_ERROR and msg is None
+    np.testing.assert_array_equal(got_off, exp_off)
+    np.testing.assert_array_equal(got_carry, exp_carry)
+
+
+def test_noalloc_reports_an_index_out_of_range_like_the_pooled_entry_point():
+    from awkward_gb300 import _abi
+
+    off, soff, idx = _case(5_000, 14)
+    idx = idx.copy()
+    # one index past its list's length (the list owning slice position 7)
+    owner = np.searchsorted(soff, 7, side="right") - 1
+    idx[7] = off[owner + 1] - off[owner]
+    rc_a, err_a, _, _ = _run(_noalloc_fn(), off, soff, idx)
+    rc_b, err_b, _, _ = _run(_abi.cfunc(POOLED), off, soff, idx)
+    msg, _, _ = _oracle(off, soff, idx)
+    assert rc_a == 0 and rc_b == 0
+    assert msg is not None and "index out of range" in msg
+    # invocation index 0, message 4 of awkward's jagged_apply kernel
+    assert err_a == err_b == 4, (hex(err_a), hex(err_b))
