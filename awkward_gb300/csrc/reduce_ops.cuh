@@ -568,6 +568,63 @@ __device__ __forceinline__ FxAcc run_short(const FixedSumOp<IN>& op, const IN* p
   }
 }
 
+// ---------------------------------------------------------------- whole short lists
+// The output of a whole list of n <= kShortList float64 elements at p
+// (global index st) for the lane-per-list rounds of seg_reduce_kernel: the
+// largest raw key in one pass, with nothing but the key kept per element.
+// The raw key is a bijection, so the winner's bits are the key mapped back,
+// and the output equals finalize(run_short(...)) bit for bit whenever *fast
+// stays true -- that is, unless the winner is a zero or a NaN (or, for the
+// arg-reducers, the list starts with a NaN), where the caller reruns
+// run_short's exact path.
+template <bool MAX>
+struct LaneFinal<ExtremumOp<double, MAX>> : std::true_type {};
+template <bool MAX>
+struct LaneFinal<ArgExtremumOp<double, MAX>> : std::true_type {};
+
+// 0 < |b| <= inf: the winner is neither a zero nor a NaN
+__device__ __forceinline__ bool raw_winner_exact(long long b) {
+  return (unsigned long long)((b & 0x7fffffffffffffffLL) - 1) < 0x7ff0000000000000ULL;
+}
+
+template <bool MAX>
+__device__ __forceinline__ double lane_final(const ExtremumOp<double, MAX>& op, const double* p,
+                                             int n, long long, bool& fast) {
+  if (n <= 0) return op.ident;
+  const long long* q = reinterpret_cast<const long long*>(p);
+  long long best = kKeyLow;  // the first element is always taken
+  for (int i = 0; i < n; i++) {
+    const long long k = MAX ? f64_raw_key(__ldg(q + i)) : ~f64_raw_key(__ldg(q + i));
+    best = k > best ? k : best;
+  }
+  const long long bits = f64_raw_key(MAX ? best : ~best);  // the raw key is an involution
+  fast = raw_winner_exact(bits);
+  // identity -inf (max) / +inf (min): every non-NaN winner is the output
+  // (an infinite winner equal to the identity has the identity's bits)
+  if (__double_as_longlong(op.ident) == (MAX ? (long long)0xfff0000000000000ULL : 0x7ff0000000000000LL))
+    return __longlong_as_double(bits);
+  return op.finalize({f64_dir_key<MAX>(__longlong_as_double(bits)), bits, 0}, 0);
+}
+
+template <bool MAX>
+__device__ __forceinline__ int64_t lane_final(const ArgExtremumOp<double, MAX>&, const double* p,
+                                              int n, long long st, bool& fast) {
+  if (n <= 0) return -1;
+  const long long* q = reinterpret_cast<const long long*>(p);
+  long long best = kKeyLow;
+  int at = 0;
+  for (int i = 0; i < n; i++) {
+    const long long k = MAX ? f64_raw_key(__ldg(q + i)) : ~f64_raw_key(__ldg(q + i));
+    if (k > best) {
+      best = k;
+      at = i;
+    }
+  }
+  const long long bits = f64_raw_key(MAX ? best : ~best);
+  fast = raw_winner_exact(bits) && !is_nan(__longlong_as_double(__ldg(q)));
+  return st + at;
+}
+
 // ---------------------------------------------------------------- warp runs
 // Reduce elements [s, e) of list `li` (first element st) with a group of G
 // lanes (G = 32: the whole warp; G = 8: four groups, four lists at once),

@@ -142,6 +142,97 @@ template <int G, class Op>
 __device__ typename Op::Acc run_coop(const Op& op, const store_t<typename Op::In>* x, long long s,
                                      long long e, long long st, long long li);
 
+// The lanes' lists li = base + lane of one round of a warp range (st, en:
+// the list's offsets; `act`: li <= last_list), read from global memory:
+// lists of at most kShortList elements by their lane, longer ones by groups
+// of 8 lanes or the whole warp.  Lists that end in the range are emitted; the
+// partials of the giant list crossing the range start (head) or open at its
+// end (I1, tail) go to `rec`; a list of at most kAbsorb elements open at the
+// end is left to the range where it ends.
+template <class Op, class Emit>
+__device__ __forceinline__ void seg_direct_lists(const Op& op,
+                                                 const store_t<typename Op::In>* __restrict__ x,
+                                                 long long base, bool act, long long st,
+                                                 long long en, long long I1, long long J0,
+                                                 long long J1, Emit& emit,
+                                                 RangeRecord<typename Op::Acc>& rec) {
+  const int lane = threadIdx.x & 31;
+  const long long li = base + lane;
+  long long s0 = 0, e = 0;
+  bool skip = false;
+  if (act) {
+    const bool small = en - st <= kAbsorb;  // reduced whole by the range where it ends
+    s0 = (st < J0 && !small) ? J0 : st;
+    e = li == I1 ? J1 : en;
+    skip = li == I1 && small;  // the range where it ends takes all of it
+    if (e < s0) e = s0;
+  }
+  typename Op::Acc acc = op.identity();
+  if (act && !skip && e - s0 <= kShortList) acc = run_short(op, x + s0, (int)(e - s0), s0, st, li);
+  const bool longer = act && !skip && e - s0 > kShortList;
+  // medium lists: four at a time, 8 lanes each (four load chains in flight)
+  unsigned med = __ballot_sync(0xffffffffu, longer && e - s0 <= kMediumList);
+  unsigned coop = __ballot_sync(0xffffffffu, longer) & ~med;
+  while (med) {
+    int src = -1;  // the list of this lane's group
+#pragma unroll
+    for (int g = 0; g < 4; g++) {
+      const int cand = med ? __ffs(med) - 1 : -1;
+      if (cand >= 0) med &= med - 1;
+      if ((lane >> 3) == g) src = cand;
+    }
+    const int from = src < 0 ? 0 : src;
+    long long s2 = __shfl_sync(0xffffffffu, s0, from);
+    long long e2 = __shfl_sync(0xffffffffu, e, from);
+    const long long st2 = __shfl_sync(0xffffffffu, st, from);
+    if (src < 0) e2 = s2;  // an idle group reduces nothing
+    const typename Op::Acc a2 = run_coop<8>(op, x, s2, e2, st2, base + from);
+    // the owner lane takes its list's result from the first lane of its group
+    int owner_group = -1;
+#pragma unroll
+    for (int g = 0; g < 4; g++)
+      if (__shfl_sync(0xffffffffu, src, g * 8) == lane) owner_group = g;
+    const typename Op::Acc mine = shfl_idx(a2, owner_group < 0 ? 0 : owner_group * 8);
+    if (owner_group >= 0) acc = mine;
+  }
+  while (coop) {  // longer lists: the whole warp, strided (coalesced)
+    const int src = __ffs(coop) - 1;
+    coop &= coop - 1;
+    const long long s2 = __shfl_sync(0xffffffffu, s0, src);
+    const long long e2 = __shfl_sync(0xffffffffu, e, src);
+    const long long st2 = __shfl_sync(0xffffffffu, st, src);
+    const long long l2 = base + src;
+    const typename Op::Acc a2 = run_coop<32>(op, x, s2, e2, st2, l2);
+    if (lane == src) acc = a2;
+  }
+  if (act && !skip) {
+    if (li == I1) {
+      rec.tail_acc = acc;  // a giant list continues in the next range
+    } else if (s0 > st) {
+      rec.head_acc = acc;  // the end of a giant list that began earlier
+    } else {
+      emit(li, acc);
+    }
+  }
+}
+
+// The records of a warp range (lane 0): the giant list crossing its start
+// and the one open at its end.
+template <class Op>
+__device__ __forceinline__ void seg_range_records(const Op& op,
+                                                  const int64_t* __restrict__ offsets,
+                                                  long long nlists, long long I0, long long I1,
+                                                  long long J0,
+                                                  RangeRecord<typename Op::Acc>& rec) {
+  const long long st0 = __ldg(offsets + I0);
+  const bool head = I0 < I1 && st0 < J0 && __ldg(offsets + I0 + 1) - st0 > kAbsorb;
+  rec.head_list = head ? I0 : -1;
+  const bool tail = I1 < nlists && __ldg(offsets + I1 + 1) - __ldg(offsets + I1) > kAbsorb;
+  rec.tail_list = tail ? I1 : -1;
+  rec.tail_fresh = (tail && __ldg(offsets + I1) >= J0) ? 1 : 0;
+  if (!tail) rec.tail_acc = op.identity();
+}
+
 // Reduce the lists of merge-path diagonal range [d0, d1) of one array
 // (whole warp).  emit(list, acc) delivers each list reduced entirely here;
 // the partials of lists crossing the range ends go to `rec`.
@@ -165,78 +256,18 @@ __device__ __forceinline__ void seg_reduce_range(const Op& op,
   for (long long base = I0; base <= last_list; base += 32) {
     const long long li = base + lane;
     const bool act = li <= last_list;
-    long long st = 0, s0 = 0, e = 0;
-    bool skip = false;
+    long long st = 0, en = 0;
     if (act) {
       st = __ldg(offsets + li);
-      const long long en = __ldg(offsets + li + 1);
-      const bool small = en - st <= kAbsorb;  // reduced whole by the range where it ends
-      s0 = (st < J0 && !small) ? J0 : st;
-      e = li == I1 ? J1 : en;
-      skip = li == I1 && small;  // the range where it ends takes all of it
-      if (e < s0) e = s0;
+      en = __ldg(offsets + li + 1);
     }
     if (li + 32 <= last_list) {  // the next round's offsets in flight (result never read)
       long long dd;
       asm volatile("ld.global.nc.b64 %0, [%1];" : "=l"(dd) : "l"(offsets + li + 32));
     }
-    typename Op::Acc acc = op.identity();
-    if (act && !skip && e - s0 <= kShortList) acc = run_short(op, x + s0, (int)(e - s0), s0, st, li);
-    const bool longer = act && !skip && e - s0 > kShortList;
-    // medium lists: four at a time, 8 lanes each (four load chains in flight)
-    unsigned med = __ballot_sync(0xffffffffu, longer && e - s0 <= kMediumList);
-    unsigned coop = __ballot_sync(0xffffffffu, longer) & ~med;
-    while (med) {
-      int src = -1;  // the list of this lane's group
-#pragma unroll
-      for (int g = 0; g < 4; g++) {
-        const int cand = med ? __ffs(med) - 1 : -1;
-        if (cand >= 0) med &= med - 1;
-        if ((lane >> 3) == g) src = cand;
-      }
-      const int from = src < 0 ? 0 : src;
-      long long s2 = __shfl_sync(0xffffffffu, s0, from);
-      long long e2 = __shfl_sync(0xffffffffu, e, from);
-      const long long st2 = __shfl_sync(0xffffffffu, st, from);
-      if (src < 0) e2 = s2;  // an idle group reduces nothing
-      const typename Op::Acc a2 = run_coop<8>(op, x, s2, e2, st2, base + from);
-      // the owner lane takes its list's result from the first lane of its group
-      int owner_group = -1;
-#pragma unroll
-      for (int g = 0; g < 4; g++)
-        if (__shfl_sync(0xffffffffu, src, g * 8) == lane) owner_group = g;
-      const typename Op::Acc mine = shfl_idx(a2, owner_group < 0 ? 0 : owner_group * 8);
-      if (owner_group >= 0) acc = mine;
-    }
-    while (coop) {  // longer lists: the whole warp, strided (coalesced)
-      const int src = __ffs(coop) - 1;
-      coop &= coop - 1;
-      const long long s2 = __shfl_sync(0xffffffffu, s0, src);
-      const long long e2 = __shfl_sync(0xffffffffu, e, src);
-      const long long st2 = __shfl_sync(0xffffffffu, st, src);
-      const long long l2 = base + src;
-      const typename Op::Acc a2 = run_coop<32>(op, x, s2, e2, st2, l2);
-      if (lane == src) acc = a2;
-    }
-    if (act && !skip) {
-      if (li == I1) {
-        rec.tail_acc = acc;  // a giant list continues in the next range
-      } else if (s0 > st) {
-        rec.head_acc = acc;  // the end of a giant list that began earlier
-      } else {
-        emit(li, acc);
-      }
-    }
+    seg_direct_lists(op, x, base, act, st, en, I1, J0, J1, emit, rec);
   }
-  if (lane == 0) {
-    const long long st0 = __ldg(offsets + I0);
-    const bool head = I0 < I1 && st0 < J0 && __ldg(offsets + I0 + 1) - st0 > kAbsorb;
-    rec.head_list = head ? I0 : -1;
-    const bool tail = I1 < nlists && __ldg(offsets + I1 + 1) - __ldg(offsets + I1) > kAbsorb;
-    rec.tail_list = tail ? I1 : -1;
-    rec.tail_fresh = (tail && __ldg(offsets + I1) >= J0) ? 1 : 0;
-    if (!tail) rec.tail_acc = op.identity();
-  }
+  if (lane == 0) seg_range_records(op, offsets, nlists, I0, I1, J0, rec);
 }
 
 // Number of warp ranges an array of nlists lists and E elements is split
@@ -252,6 +283,21 @@ __host__ __device__ __forceinline__ int seg_ranges(long long nlists, long long E
   return seg_ranges_min(nlists, E, W, kMinRangeItems);
 }
 
+// The reducers with a direct finisher for a whole list of at most
+// kShortList elements (lane_final, defined with them in reduce_ops.cuh).
+template <class Op>
+struct LaneFinal : std::false_type {};
+
+// The per-array kernel.  A warp walks its merge-path range 32 lists per
+// round, one lane per list.  The lanes' list ends are one coalesced 8-byte
+// load per round (starts come from the lane below), and a round whose lists
+// all end inside the range with at most kShortList elements each -- nearly
+// every round of short-list data -- is finished by the lanes alone: each
+// computes its list's output with the reducer's short-run arithmetic
+// (lane_final where the reducer has one, else finalize(run_short)) and
+// stores it.  Other rounds (a list longer than kShortList, the giant list
+// crossing the range start, the list open at its end) take the general
+// per-round path.  Both give the same bits for a list.
 template <class Op>
 __global__ void __launch_bounds__(kSegBlock, kSegMinBlocks)
     seg_reduce_kernel(Op op, const store_t<typename Op::In>* __restrict__ x,
@@ -260,6 +306,7 @@ __global__ void __launch_bounds__(kSegBlock, kSegMinBlocks)
                       int W, uint64_t inv, uint64_t* err) {
   (void)inv;
   (void)err;
+  const int lane = threadIdx.x & 31;
   const int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
   const long long e0 = __ldg(offsets);
   const long long eN = __ldg(offsets + nlists);
@@ -268,9 +315,42 @@ __global__ void __launch_bounds__(kSegBlock, kSegMinBlocks)
   const int Weff = seg_ranges(nlists, E, W);
   if (w >= Weff) return;
   const long long d0 = D * w / Weff, d1 = D * (w + 1) / Weff;
-  seg_reduce_range(
-      op, x, offsets, nlists, e0, E, d0, d1,
-      [&](long long li, const typename Op::Acc& a) { out[li] = op.finalize(a, li); }, records[w]);
+  RangeRecord<typename Op::Acc>& rec = records[w];
+  auto emit = [&](long long li, const typename Op::Acc& a) { out[li] = op.finalize(a, li); };
+  // both ends at once: lanes 0-15 search d0, lanes 16-31 search d1
+  const bool upper = lane >= 16;
+  const long long split = mp_search_half(offsets, nlists, e0, E, upper ? d1 : d0,
+                                         upper ? 0xffff0000u : 0x0000ffffu);
+  const long long I0 = __shfl_sync(0xffffffffu, split, 0);
+  const long long I1 = __shfl_sync(0xffffffffu, split, 16);
+  const long long J0 = e0 + (d0 - I0), J1 = e0 + (d1 - I1);
+  const long long last_list = I1 < nlists ? I1 : I1 - 1;  // I1 itself is the tail, if any
+  long long carry = __ldg(offsets + I0);  // start of the round's first list
+  for (long long base = I0; base <= last_list; base += 32) {
+    const long long li = base + lane;
+    const bool act = li <= last_list;
+    const long long en = __ldg(offsets + (act ? li : last_list) + 1);
+    long long st = __shfl_up_sync(0xffffffffu, en, 1);
+    if (lane == 0) st = carry;
+    carry = __shfl_sync(0xffffffffu, en, 31);
+    const long long n = en - st;
+    // every list of the round whole, short and ending in the range (I1 is
+    // the list open at the range end)
+    const bool plain = li != I1 && (unsigned long long)n <= (unsigned long long)kShortList;
+    if (__all_sync(0xffffffffu, !act || plain)) {
+      const int m = act ? (int)n : 0;
+      typename Op::Out r;
+      bool fast = true;
+      if constexpr (LaneFinal<Op>::value) r = lane_final(op, x + st, m, st, fast);
+      else r = op.finalize(run_short(op, x + st, m, st, st, li), li);
+      if (!__all_sync(0xffffffffu, fast) && !fast)
+        r = op.finalize(run_short(op, x + st, m, st, st, li), li);
+      if (act) out[li] = r;
+    } else {
+      seg_direct_lists(op, x, base, act, st, en, I1, J0, J1, emit, rec);
+    }
+  }
+  if (lane == 0) seg_range_records(op, offsets, nlists, I0, I1, J0, rec);
 }
 
 // Giant lists (more than kAbsorb elements) that cross warp ranges: one warp
