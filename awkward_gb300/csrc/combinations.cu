@@ -126,6 +126,125 @@ __device__ __forceinline__ long long binom3(long long m) {
   return m < 3 ? 0 : m * (m - 1) * (m - 2) / 6;
 }
 
+// Pairs (N = 2) or triples (N = 3) of one warp's share [qa, qb) of a tile's
+// output slots, tile-local positions in 32 bits (the tile has fewer than
+// 2^31 - 64 tuples).  Each step covers 256 consecutive slots: lane l owns
+// slots g + 8l .. g + 8l + 7, finds the list of its first slot by binary
+// search over the tile's offsets, unranks that slot (closed forms, as the
+// per-slot path) and steps through the next seven by the lexicographic
+// successor -- (i, j) -> (i, j + 1), or (i + 1, i + 2) after the row's last
+// pair; triples likewise -- moving to the next non-empty list where one
+// ends.  The tuples pass through the warp's padded stage `sw` in shared
+// memory (kSuccStage words, one output array at a time) so that the stores to
+// global memory are coalesced.
+constexpr int kSuccStep = 256, kSuccPer = 8;  // slots per warp step, per lane
+constexpr int kSuccStage = kSuccStep + kSuccStep / kSuccPer;  // padded: slot j at j + j/8
+
+template <int N>
+__device__ __forceinline__ void fill_successors(long long* __restrict__ sw,
+                                                const TileSmem& sm, const int* __restrict__ loc32,
+                                                const long long* __restrict__ s_start,
+                                                const long long* __restrict__ s_size,
+                                                int64_t* const* s_ptr, long long prefix, int qa,
+                                                int qb, bool replacement) {
+  constexpr int kStep = kSuccStep, kPer = kSuccPer;
+  const int lane = threadIdx.x & 31;
+  const int shift = replacement ? 1 : 0;
+  int r = tile_find(sm, qa);
+  for (int g = qa; g < qb; g += kStep) {
+    const int q0 = g + kPer * lane;
+    long long v[N][kPer];
+    int rl = r;
+    if (q0 < qb) {
+      int hi = kTileLists - 1;  // largest rl with loc32[rl] <= q0: the list of slot q0
+      while (rl < hi) {
+        const int mid = (rl + hi + 1) >> 1;
+        if (loc32[mid] <= q0) rl = mid;
+        else hi = mid - 1;
+      }
+      int s = (int)s_size[rl];
+      long long base = s_start[rl];
+      int cend = loc32[rl + 1];
+      const int rank = q0 - loc32[rl];
+      int a, b, c = 0;
+      if constexpr (N == 2) {
+        if (s < (1 << 15)) {
+          unrank2_small(s, rank, &a, &b);
+        } else {
+          long long A, B;
+          unrank2(s, rank, &A, &B);
+          a = (int)A;
+          b = (int)B;
+        }
+      } else {
+        // first element: largest v with C(s,3) - C(s-v,3) <= rank; C(s,3) < 2^31
+        auto c3 = [](long long m) { return m < 3 ? 0ll : m * (m - 1) * (m - 2) / 6; };
+        const long long tot = c3(s);
+        int lo = 0, hi2 = s - 3;
+        while (lo < hi2) {
+          const int mid = (lo + hi2 + 1) >> 1;
+          if (tot - c3(s - mid) <= rank) lo = mid;
+          else hi2 = mid - 1;
+        }
+        int a2, b2;
+        unrank2_small(s - lo - 1, (int)(rank - (tot - c3(s - lo))), &a2, &b2);
+        a = lo;
+        b = lo + 1 + a2;
+        c = lo + 1 + b2;
+      }
+#pragma unroll
+      for (int k = 0; k < kPer; k++) {
+        const int q = q0 + k;
+        v[0][k] = base + a;
+        v[1][k] = base + b - shift;
+        if constexpr (N == 3) v[2][k] = base + c - 2 * shift;
+        if (k + 1 < kPer && q + 1 < qb) {
+          if (q + 1 == cend) {  // the next non-empty list
+            do {
+              rl++;
+            } while (loc32[rl + 1] <= q + 1);
+            s = (int)s_size[rl];
+            base = s_start[rl];
+            cend = loc32[rl + 1];
+            a = 0;
+            b = 1;
+            c = 2;
+          } else if constexpr (N == 2) {
+            if (++b == s) {
+              ++a;
+              b = a + 1;
+            }
+          } else {
+            if (++c == s) {
+              if (++b == s - 1) {
+                ++a;
+                b = a + 1;
+              }
+              c = b + 1;
+            }
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int o = 0; o < N; o++) {
+      __syncwarp();
+      if (q0 < qb) {
+#pragma unroll
+        for (int k = 0; k < kPer; k++) sw[(kPer + 1) * lane + k] = v[o][k];
+      }
+      __syncwarp();
+      int64_t* __restrict__ outp = s_ptr[o] + prefix;
+#pragma unroll
+      for (int m = 0; m < kStep / 32; m++) {
+        const int j = 32 * m + lane;
+        if (g + j < qb) outp[g + j] = sw[j + (j >> 3)];
+      }
+    }
+    r = __shfl_sync(0xffffffffu, rl, 31);  // lists only increase
+  }
+}
+
 template <class C>
 __global__ void __launch_bounds__(kTileBlock)
     combinations_kernel(int64_t** __restrict__ tocarry, int64_t* __restrict__ toindex,
@@ -174,75 +293,11 @@ __global__ void __launch_bounds__(kTileBlock)
     const int t32 = (int)total;
     const int qa = (int)((long long)t32 * warp / kWarps), qb = (int)((long long)t32 * (warp + 1) / kWarps);
     if (qa >= qb) return;
-    int64_t* __restrict__ out0 = s_ptr[0];
-    int64_t* __restrict__ out1 = s_ptr[1];
-    int64_t* __restrict__ out2 = n == 3 ? s_ptr[2] : nullptr;
-    const int shift = replacement ? 1 : 0;
-    int r = tile_find(sm, qa);
-    for (int g = qa; g < qb; g += 32) {
-      while (loc32[r + 1] <= g) r++;
-      const int q = g + lane;
-      int rnext;
-      int rl = warp_step_lists(loc32, r, g, lane, &rnext);
-      if (rl < 0) {
-        rl = r;
-        if (q < qb)
-          while (loc32[rl + 1] <= q) rl++;
-        rnext = r;
-      }
-      r = rnext;
-      if (q >= qb) continue;
-      const int rank = q - loc32[rl];
-      const long long s = s_size[rl];
-      const long long base = s_start[rl];
-      if (n == 3) {
-        long long p0, p1, p2;
-        if (s < 1024) {  // C(s,3) < 2^31: every product in 32 bits
-          const int si = (int)s;
-          auto c3 = [](int m) { return m < 3 ? 0 : (m * (m - 1) * (m - 2)) / 6; };
-          const int tot = c3(si);
-          int lo = 0, hi = si - 3;
-          while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (tot - c3(si - mid) <= rank) lo = mid;
-            else hi = mid - 1;
-          }
-          int a2, b2;
-          unrank2_small(si - lo - 1, rank - (tot - c3(si - lo)), &a2, &b2);
-          p0 = lo;
-          p1 = lo + 1 + a2;
-          p2 = lo + 1 + b2;
-        } else {
-          const long long tot = binom3(s);
-          long long lo = 0, hi = s - 3;
-          while (lo < hi) {
-            const long long mid = (lo + hi + 1) >> 1;
-            if (tot - binom3(s - mid) <= rank) lo = mid;
-            else hi = mid - 1;
-          }
-          long long a2, b2;
-          unrank2(s - lo - 1, rank - (tot - binom3(s - lo)), &a2, &b2);
-          p0 = lo;
-          p1 = lo + 1 + a2;
-          p2 = lo + 1 + b2;
-        }
-        out0[prefix + q] = base + p0;
-        out1[prefix + q] = base + p1 - shift;
-        out2[prefix + q] = base + p2 - 2 * shift;
-        continue;
-      }
-      long long a, b;
-      if (s < (1ll << 15)) {
-        int ai, bi;
-        unrank2_small((int)s, rank, &ai, &bi);
-        a = ai;
-        b = bi;
-      } else {
-        unrank2(s, rank, &a, &b);
-      }
-      out0[prefix + q] = base + a;
-      out1[prefix + q] = base + b - shift;
-    }
+    __shared__ long long stage[kWarps][kSuccStage];  // the warp's output stage
+    if (n == 2)
+      fill_successors<2>(stage[warp], sm, loc32, s_start, s_size, s_ptr, prefix, qa, qb, replacement);
+    else
+      fill_successors<3>(stage[warp], sm, loc32, s_start, s_size, s_ptr, prefix, qa, qb, replacement);
     return;
   }
   const long long qa = total * warp / kWarps, qb = total * (warp + 1) / kWarps;
