@@ -56,6 +56,35 @@ def make_c1(n, seed):
     return off, x
 
 
+def make_c1_shard(n, rank, world):
+    """This rank's shard of one global C1 array of world * n lists.
+
+    The global list lengths come from seed 0 on every rank, the shard is the
+    rank's balanced list range (awkward_gb300.shard.local_shard's bounds), and
+    its content is drawn from a per-rank seed.  Returns (local offsets from 0,
+    content, global offsets slice of the shard, first global list).  With
+    world == 1 this is exactly make_c1(n, 0).
+    """
+    if world == 1:
+        off, x = make_c1(n, 0)
+        return off, x, off, 0
+    from awkward_gb300 import shard
+
+    rng = np.random.default_rng(0)
+    N = n * world
+    L = rng.poisson(8, N).astype(np.int64)
+    L[rng.random(N) < 0.01] = 0
+    goff = np.empty(N + 1, np.int64)
+    goff[0] = 0
+    np.cumsum(L, out=goff[1:])
+    b = shard.shard_bounds(goff, world)
+    l0, l1 = int(b[rank]), int(b[rank + 1])
+    gslice = goff[l0:l1 + 1]
+    local = gslice - gslice[0]
+    x = np.random.default_rng(1000 + rank).standard_normal(int(local[-1]))
+    return local, x, gslice, l0
+
+
 def algorithmic_bytes(n, e):
     """Per reducer launch: content + offsets read, one 8-byte result per list."""
     return 8 * e + 8 * (n + 1) + 8 * n
@@ -512,9 +541,36 @@ def measure_c5(dev, reps, warmup, n_lists=4_000_000):
             step()
         torch.cuda.synchronize(dev)
         ms = _time_ms(step, reps, stream)
-        res[name] = {"fwd_bwd_ms": round(ms, 4)}
+        nbytes = c5_bytes(name, n_lists, E, 4)
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        res[name] = {"fwd_bwd_ms": round(ms, 4), "algorithmic_bytes": nbytes,
+                     "gbs": round(gbs, 1), "frac": round(gbs / measured_peak()[0], 4)}
     res["sizes"] = {"lists": n_lists, "elements": E}
+    res["bytes"] = ("forward + backward, each value read or written once per kernel that must "
+                    "touch it: sum 8E+24N+16; max 12E+40N+16; softmax 20E+16N+16 (itemsize 4)")
     return res
+
+
+def c5_bytes(name, n, e, itemsize):
+    """Algorithmic bytes of one forward + backward of a C5 operation.
+
+    sum: forward reads x and offsets, writes one value per list; backward
+    reads the list gradients and offsets, writes one gradient per element.
+    max: forward runs max and argmax (x and offsets each, values + int64
+    indices out); backward reads gradients and indices, writes every element
+    gradient.  softmax: forward reads x, writes y; backward (recomputing the
+    maxima and normalisers from x) reads gradient and x, writes the input
+    gradient; offsets read by each kernel.
+    """
+    off = 8 * (n + 1)
+    if name == "sum":
+        return (itemsize * e + off + itemsize * n) + (itemsize * n + off + itemsize * e)
+    if name == "max":
+        return ((itemsize * e + off + itemsize * n) + (itemsize * e + off + 8 * n)
+                + (itemsize * n + 8 * n + itemsize * e))
+    if name == "softmax":
+        return (2 * itemsize * e + off) + (3 * itemsize * e + off)
+    raise KeyError(name)
 
 
 def measure_sort(be, dev, reps, warmup, n_lists=10_000_000):
@@ -660,7 +716,7 @@ def run_gb300(args):
     k_max = be["awkward_reduce_max", np.float64, np.float64, np.int64]
     k_arg = be["awkward_reduce_argmax", np.int64, np.float64, np.int64, np.int64]
 
-    off_h, x_h = make_c1(args.lists, rank)
+    off_h, x_h, goff_h, first_list = make_c1_shard(args.lists, rank, world)
     n, e = len(off_h) - 1, len(x_h)
     off = torch.from_numpy(off_h).to(dev)
     x = torch.from_numpy(x_h).to(dev)
@@ -746,6 +802,15 @@ def run_gb300(args):
                    for a, b in zip(outs_pin, dev_outs))
     e2e_value = world * step_bytes / (ms_e2e * 1e-3) / 1e9
 
+    # the one collective of sharded execution: local offsets rebased by the
+    # exclusive prefix of the shards' totals (an allgather over NCCL), which
+    # must give the global offsets of this rank's lists
+    from awkward_gb300 import shard
+
+    rebased = shard.rebase_offsets(off_h)
+    shard_info = {"first_list": first_list, "lists": n, "elements": e,
+                  "rebase_ok": bool(reduce_max(0.0 if np.array_equal(rebased, goff_h) else 1.0)
+                                    == 0.0)}
     dominant = max(per, key=per.get)
     peak, peak_kind = measured_peak()
     achieved = algorithmic_bytes(n, e) / (per[dominant] * 1e-3) / 1e9
@@ -768,6 +833,7 @@ def run_gb300(args):
                 "path": f"awkward_gb300.pipeline.reduce_host, {args.chunks} chunks",
                 "outputs_equal_device_path": e2e_same},
         "gpu_launches": args.steps * 3 * 2,
+        "shard": shard_info,
         "clocks": sampler.summary(),
     }
     if rank == 0 and not args.no_extras:

@@ -63,3 +63,22 @@ def test_reference_arm_under_torchrun_prints_on_rank_zero_only():
     lines = _json_lines(r.stdout)
     assert len(lines) == 1
     assert lines[0]["impl"] == "reference" and lines[0]["n_gpus"] == 2
+
+
+def test_bench_shards_concatenate_to_one_global_array():
+    sys.path.insert(0, ROOT)
+    import numpy as np
+
+    import bench
+
+    world = 3
+    parts = [bench.make_c1_shard(5000, r, world) for r in range(world)]
+    glob = np.concatenate([parts[0][2]] + [p[2][1:] for p in parts[1:]])
+    assert glob[0] == 0 and len(glob) == world * 5000 + 1
+    for r, (local, x, gslice, l0) in enumerate(parts):
+        np.testing.assert_array_equal(local, gslice - gslice[0])
+        assert len(x) == local[-1] and (r == 0 or l0 > 0)
+    off1, x1, g1, l01 = bench.make_c1_shard(5000, 0, 1)
+    off0, x0 = bench.make_c1(5000, 0)
+    np.testing.assert_array_equal(off1, off0) and np.testing.assert_array_equal(x1, x0)
+    assert l01 == 0
