@@ -115,6 +115,23 @@ EXTENSIONS["awkward_gb300_reduce_sum_max_argmax_host_float64"] = (
      ("double*", "d_x"), ("int64_t*", "d_offsets"), ("double*", "d_sum"), ("double*", "d_max"),
      ("int64_t*", "d_argmax"), ("int64_t", "chunks"), ("void*", "stream")], "pipeline")
 
+_FUSED_COMMENT = """elementwise map fused into the segmented reduction (no counterpart in
+kernel-specification.yml; awkward evaluates such chains as an elementwise
+kernel followed by a reducer, or through its lazy fusion backend).
+float64 content x (and y), int64 offsets [nlists + 1] (need not start at
+0), indexed globally.  map: 0 x, 1 x*y, 2 x*x, 3 |x| (y may be NULL unless
+map is 1).  reduce: 0 sum, 1 max (identity -inf), 2 min (identity +inf)
+into double out[nlists]; 3 argmax, 4 argmin into int64 out[nlists]
+(global indices, -1 for empty lists).  Equal to awkward_reduce_* on the
+materialised mapped values (sums within the reducers' bound).  Other
+map or reduce values, or map 1 without y, return cudaErrorInvalidValue."""
+
+EXTENSIONS["awkward_gb300_fused_reduce_float64"] = (
+    [("void*", "out"), ("const double*", "x"), ("const double*", "y"),
+     ("const int64_t*", "offsets"), ("int64_t", "nlists"), ("int64_t", "map"),
+     ("int64_t", "reduce"), ("uint64_t", "invocation_index"), ("uint64_t*", "err_code"),
+     ("void*", "stream")], "fused")
+
 _SELFTEST_COMMENT = """self-test of the failure report (no counterpart in awkward): one warp
 runs the decoupled look-back of the scan kernels on tile 1 of a fresh
 scan whose tile 0 never publishes, with a spin limit of `spin_limit`
@@ -130,14 +147,15 @@ EXTENSIONS["awkward_gb300_selftest_lookback_timeout"] = (
 
 GROUP_COMMENTS = {"noalloc": _NOALLOC_COMMENT, "autograd": _AUTOGRAD_COMMENT,
                   "jagged": _JAGGED_COMMENT, "batch": _BATCH_COMMENT,
-                  "pipeline": _PIPELINE_COMMENT, "selftest": _SELFTEST_COMMENT}
+                  "pipeline": _PIPELINE_COMMENT, "fused": _FUSED_COMMENT,
+                  "selftest": _SELFTEST_COMMENT}
 GROUP_DEFINES = {"noalloc": ["#define AWKWARD_GB300_NOALLOC_MAX_LISTS 67108864LL"]}
 
 
 def header_lines():
     """Declarations of the extension entry points, grouped, for the C header."""
     out = []
-    for group in ("noalloc", "jagged", "autograd", "batch", "pipeline", "selftest"):
+    for group in ("noalloc", "jagged", "autograd", "batch", "pipeline", "fused", "selftest"):
         out.append("")
         text = GROUP_COMMENTS[group].splitlines()
         out.append(f"/* ---- {text[0]}")

@@ -428,14 +428,34 @@ __device__ __forceinline__ void touch_run(const void* p, int n, int esize) {
 #pragma nv_diag_default 550
 
 // ---------------------------------------------------------------- short runs
+// Element loaders of the short-run reducers: global memory through the
+// read-only path (with "touch" loads that put a run's later sectors in
+// flight), or a run staged in shared memory.  Both give the same arithmetic.
+struct LdGlobal {
+  static constexpr bool kTouch = true;
+  template <class T>
+  __device__ __forceinline__ T operator()(const T* p) const {
+    return __ldg(p);
+  }
+};
+struct LdShared {
+  static constexpr bool kTouch = false;
+  template <class T>
+  __device__ __forceinline__ T operator()(const T* p) const {
+    return *p;
+  }
+};
+
 // Reduce n consecutive elements p[0..n) (global indices j0..j0+n) of one
-// list into a fresh accumulator.  The default steps element by element.
-template <class Op>
+// list into a fresh accumulator, elements read by `ld`.  The default steps
+// element by element.
+template <class Op, class Ld = LdGlobal>
 __device__ __forceinline__ typename Op::Acc run_short(const Op& op,
                                                       const store_t<typename Op::In>* p, int n,
-                                                      long long j0, long long st, long long li) {
+                                                      long long j0, long long st, long long li,
+                                                      Ld ld = Ld{}) {
   typename Op::Acc a = op.identity();
-  for (int i = 0; i < n; i++) a = op.step(a, __ldg(p + i), j0 + i, j0 + i == st, li);
+  for (int i = 0; i < n; i++) a = op.step(a, ld(p + i), j0 + i, j0 + i == st, li);
   return a;
 }
 
@@ -453,16 +473,16 @@ __device__ __forceinline__ bool raw_key_exact(long long k) {
   return k != 0 && k != -1 && k <= 0x7ff0000000000000LL && k >= (long long)0x800fffffffffffffULL;
 }
 
-template <bool MAX>
+template <bool MAX, class Ld = LdGlobal>
 __device__ __forceinline__ typename ExtremumOp<double, MAX>::Acc run_short(
     const ExtremumOp<double, MAX>& op, const double* p, int n, long long j0, long long st,
-    long long li) {
-  touch_run(p, n, 8);
+    long long li, Ld ld = Ld{}) {
+  if constexpr (Ld::kTouch) touch_run(p, n, 8);
   const long long* q = reinterpret_cast<const long long*>(p);
   long long best = 0;
   int at = -1;
   for (int i = 0; i < n; i++) {
-    const long long k = MAX ? f64_raw_key(__ldg(q + i)) : ~f64_raw_key(__ldg(q + i));
+    const long long k = MAX ? f64_raw_key(ld(q + i)) : ~f64_raw_key(ld(q + i));
     if (at < 0 || k > best) {
       best = k;
       at = i;
@@ -470,21 +490,21 @@ __device__ __forceinline__ typename ExtremumOp<double, MAX>::Acc run_short(
   }
   typename ExtremumOp<double, MAX>::Acc a = op.identity();
   if (at < 0) return a;
-  const long long bits = __ldg(q + at);
+  const long long bits = ld(q + at);
   if (raw_key_exact(f64_raw_key(bits))) return {f64_dir_key<MAX>(__longlong_as_double(bits)), bits, j0 + at};
-  for (int i = 0; i < n; i++) a = op.step(a, __ldg(p + i), j0 + i, j0 + i == st, li);
+  for (int i = 0; i < n; i++) a = op.step(a, ld(p + i), j0 + i, j0 + i == st, li);
   return a;
 }
 
-template <bool MAX>
+template <bool MAX, class Ld = LdGlobal>
 __device__ __forceinline__ typename ArgExtremumOp<double, MAX>::Acc run_short(
     const ArgExtremumOp<double, MAX>& op, const double* p, int n, long long j0, long long st,
-    long long li) {
+    long long li, Ld ld = Ld{}) {
   const long long* q = reinterpret_cast<const long long*>(p);
   long long best = 0;
   int at = -1;
   for (int i = 0; i < n; i++) {
-    const long long k = MAX ? f64_raw_key(__ldg(q + i)) : ~f64_raw_key(__ldg(q + i));
+    const long long k = MAX ? f64_raw_key(ld(q + i)) : ~f64_raw_key(ld(q + i));
     if (at < 0 || k > best) {
       best = k;
       at = i;
@@ -492,23 +512,23 @@ __device__ __forceinline__ typename ArgExtremumOp<double, MAX>::Acc run_short(
   }
   typename ArgExtremumOp<double, MAX>::Acc a = op.identity();
   if (at < 0) return a;
-  const long long bits = __ldg(q + at);
+  const long long bits = ld(q + at);
   // exact unless the winner is a zero or a NaN, or the run starts with a NaN
-  if (raw_key_exact(f64_raw_key(bits)) && !(j0 == st && is_nan(__ldg(p))))
+  if (raw_key_exact(f64_raw_key(bits)) && !(j0 == st && is_nan(ld(p))))
     return {f64_dir_key<MAX>(__longlong_as_double(bits)), j0 + at};
-  for (int i = 0; i < n; i++) a = op.step(a, __ldg(p + i), j0 + i, j0 + i == st, li);
+  for (int i = 0; i < n; i++) a = op.step(a, ld(p + i), j0 + i, j0 + i == st, li);
   return a;
 }
 
 // Exact float64 sum of at most 32 elements, branch-free: pass 1 finds the
 // largest exponent (and any inf/NaN), pass 2 adds the significands aligned to
 // it (|sum| < 2^58, no renormalisation needed).
-template <class IN>
+template <class IN, class Ld = LdGlobal>
 __device__ __forceinline__ FxAcc run_short(const FixedSumOp<IN>& op, const IN* p, int n,
-                                           long long, long long, long long) {
+                                           long long, long long, long long, Ld ld = Ld{}) {
   if constexpr (!std::is_same<IN, double>::value) {
     FxAcc a = op.identity();
-    for (int i = 0; i < n; i++) a = op.step(a, __ldg(p + i), 0, false, 0);
+    for (int i = 0; i < n; i++) a = op.step(a, ld(p + i), 0, false, 0);
     return a;
   } else {
     // Even positions are added in float64 (one DADD per pair, on the FP64
@@ -516,19 +536,19 @@ __device__ __forceinline__ FxAcc run_short(const FixedSumOp<IN>& op, const IN* p
     // fixed point on the integer pipes; the double partial joins the fixed
     // point once (fx_add_f64 also carries its inf/NaN).  The result stays
     // within n*eps*sum|x| of the exact sum.
-    touch_run(p, n, 8);
+    if constexpr (Ld::kTouch) touch_run(p, n, 8);
     const long long* q = reinterpret_cast<const long long*>(p);
     const int* qh = reinterpret_cast<const int*>(p) + 1;
     double dsum = 0.0;
     int ebmax = 0, ebmin = 0x7ff00000;
     int i = 0;
     for (; i + 1 < n; i += 2) {
-      dsum += __ldg(p + i);
-      const int eb = __ldg(qh + 2 * (i + 1)) & 0x7ff00000;
+      dsum += ld(p + i);
+      const int eb = ld(qh + 2 * (i + 1)) & 0x7ff00000;
       ebmax = eb > ebmax ? eb : ebmax;
       ebmin = eb < ebmin ? eb : ebmin;
     }
-    if (i < n) dsum += __ldg(p + i);
+    if (i < n) dsum += ld(p + i);
     const int half = n >> 1;  // odd positions 1, 3, ..., 2*half-1
     if (half == 0) return fx_add_f64(op.identity(), dsum);
     const int emax_f = ebmax >> 20, emin_f = ebmin >> 20;
@@ -537,7 +557,7 @@ __device__ __forceinline__ FxAcc run_short(const FixedSumOp<IN>& op, const IN* p
     if (emax_f != 0x7ff && emin_f != 0 && emax_f - emin_f < 32) {
       // every odd element normal and within 32 binades: two funnel shifts each
       for (int k = 1; k < n; k += 2) {
-        const long long b = __ldg(q + k);
+        const long long b = ld(q + k);
         const unsigned hi = (unsigned)((unsigned long long)b >> 32);
         const unsigned d = (unsigned)(emax_f - (int)((hi >> 20) & 0x7ff));
         const unsigned mh = (hi & 0xfffffu) | 0x100000u;
@@ -550,12 +570,12 @@ __device__ __forceinline__ FxAcc run_short(const FixedSumOp<IN>& op, const IN* p
       anchor = emax_f;
     } else if (emax_f == 0x7ff) {  // inf / NaN among them: the general accumulator
       FxAcc a = op.identity();
-      for (int k = 1; k < n; k += 2) a = fx_add_f64(a, __longlong_as_double(__ldg(q + k)));
+      for (int k = 1; k < n; k += 2) a = fx_add_f64(a, __longlong_as_double(ld(q + k)));
       return fx_add_f64(a, dsum);
     } else {  // zeros, subnormals or a wide exponent spread
       anchor = emax_f > 1 ? emax_f : 1;
       for (int k = 1; k < n; k += 2) {
-        const long long b = __ldg(q + k);
+        const long long b = ld(q + k);
         const int e = (int)((unsigned long long)b >> 52) & 0x7ff;
         const long long m = (b & 0xfffffffffffffLL) | ((long long)(e != 0) << 52);
         const int d = anchor - (e ? e : 1);

@@ -573,6 +573,52 @@ def c5_bytes(name, n, e, itemsize):
     raise KeyError(name)
 
 
+def measure_fused(be, dev, reps, warmup, n_lists=10_000_000):
+    """ak.sum(x * y, axis=-1) and ak.max(abs(x), axis=-1) on the C1 shape
+    (10M lists of Poisson(8), float64 N(0,1) x and y, seed 7): the fused
+    entry point against the two-kernel chain an unfused caller runs (torch's
+    elementwise kernel materialising the mapped values, then the reducer).
+    Algorithmic bytes: fused 16E (sum) or 8E (max) + 8(N+1) + 8N; the chain
+    adds the mapped array written and read back (16E)."""
+    import torch
+
+    from awkward_gb300.fused import segment_reduce
+
+    stream = torch.cuda.current_stream(dev)
+    off_h, x_h = make_c1(n_lists, 7)
+    n, E = len(off_h) - 1, len(x_h)
+    off = torch.from_numpy(off_h).to(dev)
+    x = torch.from_numpy(x_h).to(dev)
+    y = torch.randn(E, dtype=torch.float64, device=dev,
+                    generator=torch.Generator(device=dev).manual_seed(7))
+    out = torch.empty(n, dtype=torch.float64, device=dev)
+    tmp = torch.empty_like(x)
+    k_sum = be["awkward_reduce_sum", np.float64, np.float64, np.int64]
+    k_max = be["awkward_reduce_max", np.float64, np.float64, np.int64]
+    cases = {
+        "sum_x_times_y": (lambda: segment_reduce(x, off, "x*y", y, "sum", out=out),
+                          lambda: (torch.mul(x, y, out=tmp), k_sum(out, tmp, off, n)), 16),
+        "max_abs_x": (lambda: segment_reduce(x, off, "abs", None, "max", out=out),
+                      lambda: (torch.abs(x, out=tmp), k_max(out, tmp, off, n, -np.inf)), 8),
+    }
+    res = {}
+    for name, (fused, chain, ebytes) in cases.items():
+        for fn in (fused, chain):
+            for _ in range(max(warmup, 3)):
+                fn()
+        be.synchronize()
+        t_f = _time_ms(fused, reps, stream)
+        t_c = _time_ms(chain, reps, stream)
+        be.synchronize()
+        nb = ebytes * E + 8 * (n + 1) + 8 * n
+        res[name] = {"fused_ms": round(t_f, 4), "chain_ms": round(t_c, 4),
+                     "speedup": round(t_c / t_f, 2), "fused_gbs": round(nb / (t_f * 1e-3) / 1e9, 1),
+                     "fused_frac": round(nb / (t_f * 1e-3) / 1e9 / measured_peak()[0], 4),
+                     "chain_bytes": nb + 16 * E}
+    res["sizes"] = {"lists": n, "elements": E}
+    return res
+
+
 def measure_sort(be, dev, reps, warmup, n_lists=10_000_000):
     """ak.argsort / ak.sort(axis=-1) on float64: the C1 shape (10M lists of
     Poisson(8)) and a wide shape (2,000 lists of Poisson(40,000), the merged
@@ -704,6 +750,10 @@ def run_gb300(args):
     if args.only == "nonlocal":
         print(json.dumps({"nonlocal_reduce": measure_nonlocal(be, dev, args.steps, args.warmup,
                                                               args.lists or 10_000_000)}))
+        return
+    if args.only == "fused":
+        print(json.dumps({"fused_reduce": measure_fused(be, dev, args.steps, args.warmup,
+                                                        args.lists or 10_000_000)}))
         return
     if args.only == "c3":
         n2 = args.lists or 5_000_000
@@ -843,6 +893,7 @@ def run_gb300(args):
         line["c4_batched"] = measure_c4(dev)
         line["sort"] = measure_sort(be, dev, max(args.steps // 2, 5), args.warmup)
         line["nonlocal_reduce"] = measure_nonlocal(be, dev, max(args.steps // 2, 5), args.warmup)
+        line["fused_reduce"] = measure_fused(be, dev, max(args.steps // 2, 5), args.warmup)
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         line["parity"] = c1_parity(off_h, x_h, *dev_outs)
         line["cpu_baseline"] = cpu_baseline(off_h, x_h)
@@ -865,7 +916,7 @@ def main():
                    help="list chunks of the host-buffer (e2e) pipeline")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the secondary workloads (combinations, ...)")
-    p.add_argument("--only", default=None, choices=["c2", "c3", "c4", "c5", "sort", "nonlocal"],
+    p.add_argument("--only", default=None, choices=["c2", "c3", "c4", "c5", "sort", "nonlocal", "fused"],
                    help="run one secondary workload alone (profiling); --lists sets its size")
     p.add_argument("--lists", type=int, default=None,
                    help="list count (default: 10M lists for the reducers, 5M for --only c3; "

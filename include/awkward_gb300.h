@@ -780,6 +780,18 @@ int awkward_gb300_batch_plan_destroy(void* plan);
  * Returns after enqueueing; `stream` waits for the last copy back. */
 int awkward_gb300_reduce_sum_max_argmax_host_float64(double* h_sum, double* h_max, int64_t* h_argmax, const double* h_x, const int64_t* h_offsets, int64_t nlists, double* d_x, int64_t* d_offsets, double* d_sum, double* d_max, int64_t* d_argmax, int64_t chunks, void* stream);
 
+/* ---- elementwise map fused into the segmented reduction (no counterpart in
+ * kernel-specification.yml; awkward evaluates such chains as an elementwise
+ * kernel followed by a reducer, or through its lazy fusion backend).
+ * float64 content x (and y), int64 offsets [nlists + 1] (need not start at
+ * 0), indexed globally.  map: 0 x, 1 x*y, 2 x*x, 3 |x| (y may be NULL unless
+ * map is 1).  reduce: 0 sum, 1 max (identity -inf), 2 min (identity +inf)
+ * into double out[nlists]; 3 argmax, 4 argmin into int64 out[nlists]
+ * (global indices, -1 for empty lists).  Equal to awkward_reduce_* on the
+ * materialised mapped values (sums within the reducers' bound).  Other
+ * map or reduce values, or map 1 without y, return cudaErrorInvalidValue. */
+int awkward_gb300_fused_reduce_float64(void* out, const double* x, const double* y, const int64_t* offsets, int64_t nlists, int64_t map, int64_t reduce, uint64_t invocation_index, uint64_t* err_code, void* stream);
+
 /* ---- self-test of the failure report (no counterpart in awkward): one warp
  * runs the decoupled look-back of the scan kernels on tile 1 of a fresh
  * scan whose tile 0 never publishes, with a spin limit of `spin_limit`
