@@ -73,8 +73,8 @@ __device__ __forceinline__ typename OpOf<K>::type::Out* out_of(const BatchArray&
   else return a.out_argmax;
 }
 
-template <int K>
-__global__ void __launch_bounds__(kSegBlock, kSegMinBlocks)
+template <int K, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, kSegMinBlocks * kSegBlock / BLOCK)
     batch_reduce_kernel(typename OpOf<K>::type op, const BatchArray* __restrict__ arrays,
                         const int2* __restrict__ items, const int* __restrict__ order, int nitems,
                         RangeRecord<typename OpOf<K>::type::Acc>* records, unsigned* counter) {
@@ -215,6 +215,7 @@ __global__ void __launch_bounds__(kTileBlock)
 
 struct Plan {
   int narrays = 0;
+  int block = kSegBlock;  // threads per CTA of the reducer launches
   int nitems[kOps] = {};
   int blocks[kOps] = {};
   long long ntiles = 0;
@@ -228,14 +229,19 @@ struct Plan {
   uint64_t* err = nullptr;
 };
 
-template <int K>
+template <int K, int BLOCK>
 int occupancy_blocks() {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_reduce_kernel<K>, kSegBlock, 0) !=
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, batch_reduce_kernel<K, BLOCK>, BLOCK, 0) !=
           cudaSuccess ||
       n < 1)
     n = 1;
   return n;
+}
+
+template <int K>
+int occupancy_blocks(int block) {
+  return block == 128 ? occupancy_blocks<K, 128>() : occupancy_blocks<K, 256>();
 }
 
 void free_plan(Plan* p) {
@@ -260,14 +266,17 @@ cudaError_t upload(T** dst, const std::vector<T>& v) {
 
 }  // namespace
 
-constexpr long long kBatchMinRange = 4096;  // items per range when any split gives the same bits
-
 // Build a plan (set-up time: allocates and uploads its tables; synchronous).
 // Host arrays of length narrays: nlists, nelements (offsets[n] - offsets[0]),
 // maxlen (each array's longest list, -1 if unknown; may be null), and the
 // device pointers of every array's content, offsets, mask and
-// outputs.  order_mode 0: items in array order; 1: largest ranges first.
-// occupancy_div: persistent CTAs per SM = reducer occupancy / occupancy_div.
+// outputs.  The tuning knobs (the autotuner's search space):
+//   order_mode     0: items in array order; 1: largest ranges first;
+//   occupancy_div  persistent CTAs per SM = reducer occupancy / occupancy_div;
+//   range_min      items per reduction range of arrays whose lists all have
+//                  at most kAbsorb elements (any split gives their bits;
+//                  at least kMinRangeItems);
+//   block          threads per CTA of the reducer launches (128 or 256).
 // err_code: device word for bounded-wait failures of the select scan.
 GB_EXPORT int awkward_gb300_batch_plan_create(
     void** plan, int64_t narrays, const int64_t* nlists, const int64_t* nelements,
@@ -275,17 +284,22 @@ GB_EXPORT int awkward_gb300_batch_plan_create(
     const double* const* x, const int64_t* const* offsets, const uint8_t* const* mask,
     double* const* out_sum, double* const* out_max, int64_t* const* out_argmax,
     int64_t* const* out_count, int64_t* const* sel_offsets, double* const* sel_content,
-    int64_t order_mode, int64_t occupancy_div, uint64_t* err_code) {
+    int64_t order_mode, int64_t occupancy_div, int64_t range_min, int64_t block,
+    uint64_t* err_code) {
   *plan = nullptr;
-  if (narrays <= 0 || occupancy_div < 1) return (int)cudaErrorInvalidValue;
+  if (narrays <= 0 || occupancy_div < 1 || range_min < kMinRangeItems ||
+      (block != 128 && block != 256))
+    return (int)cudaErrorInvalidValue;
   Plan* p = new Plan();
   p->narrays = (int)narrays;
+  p->block = (int)block;
   p->err = err_code;
   const int sms = device_sm_count();
   const int W[kOps] = {sms * SegReduceConfig<SumOpD>::blocks_per_sm() * (kSegBlock / 32),
                        sms * SegReduceConfig<MaxOpD>::blocks_per_sm() * (kSegBlock / 32),
                        sms * SegReduceConfig<ArgOpD>::blocks_per_sm() * (kSegBlock / 32)};
-  const int occ[kOps] = {occupancy_blocks<0>(), occupancy_blocks<1>(), occupancy_blocks<2>()};
+  const int occ[kOps] = {occupancy_blocks<0>(p->block), occupancy_blocks<1>(p->block),
+                         occupancy_blocks<2>(p->block)};
   std::vector<BatchArray> arrays(narrays);
   std::vector<std::vector<int2>> items(kOps);
   std::vector<long long> tile_base(narrays + 1, 0);
@@ -298,13 +312,13 @@ GB_EXPORT int awkward_gb300_batch_plan_create(
     A.E = nelements[a] > 0 ? nelements[a] : 0;
     // Lists of at most kAbsorb elements are reduced whole by the range where
     // they end, so any split gives their bits: such arrays take ranges of at
-    // least kBatchMinRange items (fewer range searches per element).  An
+    // least range_min items (fewer range searches per element).  An
     // array with a longer list keeps its per-array split, whose partials the
     // fix-up combines in the same order.
     const bool any_split = maxlen != nullptr && maxlen[a] >= 0 && maxlen[a] <= kAbsorb;
     for (int k = 0; k < kOps; k++) {
       A.ranges[k] = nlists[a] <= 0 ? 0
-                    : any_split ? seg_ranges_min(nlists[a], A.E, W[k], kBatchMinRange)
+                    : any_split ? seg_ranges_min(nlists[a], A.E, W[k], range_min)
                                 : seg_ranges(nlists[a], A.E, W[k]);
       A.item0[k] = (int)items[k].size();
       for (int w = 0; w < A.ranges[k]; w++) items[k].push_back(make_int2(a, w));
@@ -367,23 +381,41 @@ GB_EXPORT int awkward_gb300_batch_plan_run(void* plan, void* stream) {
   op1.ident = -INFINITY;
   ArgOpD op2{};
   if (p->nitems[0] > 0) {
-    batch_reduce_kernel<0><<<p->blocks[0], kSegBlock, 0, s>>>(
-        op0, p->d_arrays, p->d_items[0], p->d_order[0], p->nitems[0],
-        static_cast<RangeRecord<SumOpD::Acc>*>(p->d_records[0]), p->d_counters + 0);
+    auto* rec0 = static_cast<RangeRecord<SumOpD::Acc>*>(p->d_records[0]);
+    if (p->block == 128)
+      batch_reduce_kernel<0, 128><<<p->blocks[0], 128, 0, s>>>(
+          op0, p->d_arrays, p->d_items[0], p->d_order[0], p->nitems[0], rec0,
+          p->d_counters + 0);
+    else
+      batch_reduce_kernel<0, 256><<<p->blocks[0], 256, 0, s>>>(
+          op0, p->d_arrays, p->d_items[0], p->d_order[0], p->nitems[0], rec0,
+          p->d_counters + 0);
     batch_fixup_kernel<0><<<(p->nitems[0] + 255) / 256, 256, 0, s>>>(
         op0, p->d_arrays, static_cast<RangeRecord<SumOpD::Acc>*>(p->d_records[0]), p->nitems[0]);
   }
   if (p->nitems[1] > 0) {
-    batch_reduce_kernel<1><<<p->blocks[1], kSegBlock, 0, s>>>(
-        op1, p->d_arrays, p->d_items[1], p->d_order[1], p->nitems[1],
-        static_cast<RangeRecord<MaxOpD::Acc>*>(p->d_records[1]), p->d_counters + 1);
+    auto* rec1 = static_cast<RangeRecord<MaxOpD::Acc>*>(p->d_records[1]);
+    if (p->block == 128)
+      batch_reduce_kernel<1, 128><<<p->blocks[1], 128, 0, s>>>(
+          op1, p->d_arrays, p->d_items[1], p->d_order[1], p->nitems[1], rec1,
+          p->d_counters + 1);
+    else
+      batch_reduce_kernel<1, 256><<<p->blocks[1], 256, 0, s>>>(
+          op1, p->d_arrays, p->d_items[1], p->d_order[1], p->nitems[1], rec1,
+          p->d_counters + 1);
     batch_fixup_kernel<1><<<(p->nitems[1] + 255) / 256, 256, 0, s>>>(
         op1, p->d_arrays, static_cast<RangeRecord<MaxOpD::Acc>*>(p->d_records[1]), p->nitems[1]);
   }
   if (p->nitems[2] > 0) {
-    batch_reduce_kernel<2><<<p->blocks[2], kSegBlock, 0, s>>>(
-        op2, p->d_arrays, p->d_items[2], p->d_order[2], p->nitems[2],
-        static_cast<RangeRecord<ArgOpD::Acc>*>(p->d_records[2]), p->d_counters + 2);
+    auto* rec2 = static_cast<RangeRecord<ArgOpD::Acc>*>(p->d_records[2]);
+    if (p->block == 128)
+      batch_reduce_kernel<2, 128><<<p->blocks[2], 128, 0, s>>>(
+          op2, p->d_arrays, p->d_items[2], p->d_order[2], p->nitems[2], rec2,
+          p->d_counters + 2);
+    else
+      batch_reduce_kernel<2, 256><<<p->blocks[2], 256, 0, s>>>(
+          op2, p->d_arrays, p->d_items[2], p->d_order[2], p->nitems[2], rec2,
+          p->d_counters + 2);
     batch_fixup_kernel<2><<<(p->nitems[2] + 255) / 256, 256, 0, s>>>(
         op2, p->d_arrays, static_cast<RangeRecord<ArgOpD::Acc>*>(p->d_records[2]), p->nitems[2]);
   }

@@ -478,38 +478,78 @@ def measure_c2(be, dev, reps, warmup, n_lists=10_000_000):
     return res
 
 
-def measure_c4(dev, narrays=4096, min_lists=1_000, max_lists=20_000, reps=5):
+def measure_c4(dev, narrays=4096, min_lists=1_000, max_lists=20_000, reps=5, full=True):
     """Batched uneven workload: sum/max/argmax/count(axis=-1) + array[mask] of
-    `narrays` float64 arrays, list counts log-uniform in [min_lists, max_lists]
-    (the [1e3, 2e6] range would hold ~270 GB of content; scaled to 2e4 at the
-    top), lengths Poisson(U(1,32)) or Geometric(0.02) per array, 5% empty.
-    Batched: one CUDA graph replay (autotuned plan).  Plain: the per-array
-    entry points array by array (wall time, host reads included)."""
+    `narrays` float64 arrays, lengths Poisson(U(1,32)) or Geometric(0.02) per
+    array, 5% empty lists, Bernoulli(0.4) masks, generated on the device from
+    per-array seeds.  Batched: one CUDA graph replay of an autotuned plan;
+    plain: the per-array entry points array by array (wall time, host reads
+    included).
+
+    scaled: list counts log-uniform in [min_lists, max_lists] (one resident
+    batch).  full: the configured range [1e3, 2e6] (about 280 GB of content),
+    run as resident waves of at most 60 GB generated on the device, one plan
+    and one graph per wave (knobs tuned on the first wave); times add up over
+    the waves."""
     import torch
 
     from awkward_gb300 import batch
 
+    def one(b, knobs, reps):
+        plan = b.plan(knobs)
+        g = b.graph(plan)
+        g.replay()
+        torch.cuda.synchronize(dev)
+        ms_b = _time_ms(g.replay, reps, torch.cuda.current_stream(dev))
+        b.check_errors()
+        batch.run_plain(b)  # warm the per-array path (pools, kernel table)
+        ms_p = batch.time_plain(b, reps=1)
+        del g
+        return ms_b, ms_p, int(b.nelements.sum()), int(b.nlists.sum())
+
+    def nbytes(E, N):
+        return 3 * (8 * E + 16 * N) + (8 * E + E + 16 * N) + 8 * int(0.4 * E)
+
+    res = {}
     b = batch.make_batch(narrays, seed=4, min_lists=min_lists, max_lists=max_lists, device=dev)
-    variant = batch.autotune(b, reps=3)
-    plan = b.plan(*variant)
-    g = b.graph(plan)
-    g.replay()
-    torch.cuda.synchronize(dev)
-    stream = torch.cuda.current_stream(dev)
-    ms_batched = _time_ms(g.replay, reps, stream)
-    b.check_errors()
-    batch.run_plain(b)  # warm the per-array path (pools, kernel table)
-    ms_plain = batch.time_plain(b, reps=1)
-    E = int(b.nelements.sum())
-    N = int(b.nlists.sum())
-    byts = 3 * (8 * E + 16 * N) + (8 * E + E + 16 * N) + 8 * int(0.4 * E)
+    t0 = time.perf_counter()
+    knobs = batch.autotune(b, reps=3)
+    tune_s = time.perf_counter() - t0
+    ms_b, ms_p, E, N = one(b, knobs, reps)
     b.close()
-    return {"arrays": narrays, "lists": N, "elements": E, "plan": {"order_mode": variant[0],
-            "occupancy_div": variant[1]},
-            "batched_ms": round(ms_batched, 3), "plain_ms": round(ms_plain, 1),
-            "speedup": round(ms_plain / ms_batched, 1),
-            "batched_gbs": round(byts / (ms_batched * 1e-3) / 1e9, 1),
-            "list_counts": f"log-uniform [{min_lists}, {max_lists}]"}
+    del b
+    res["scaled"] = {"arrays": narrays, "lists": N, "elements": E,
+                     "list_counts": f"log-uniform [{min_lists}, {max_lists}]",
+                     "knobs": knobs.__dict__, "tune_s": round(tune_s, 2),
+                     "batched_ms": round(ms_b, 3), "plain_ms": round(ms_p, 1),
+                     "speedup": round(ms_p / ms_b, 1),
+                     "batched_gbs": round(nbytes(E, N) / (ms_b * 1e-3) / 1e9, 1)}
+    if full:
+        specs = batch.batch_specs(narrays, seed=4, min_lists=1_000, max_lists=2_000_000)
+        tot_b = tot_p = 0.0
+        E = N = 0
+        fknobs = None
+        ws = batch.waves(specs, 60e9)
+        t0 = time.perf_counter()
+        for w in ws:
+            b = batch.make_wave(w, device=dev)
+            if fknobs is None:
+                fknobs = batch.autotune(b, reps=2)
+            mb, mp, e, nl = one(b, fknobs, 3)
+            tot_b += mb
+            tot_p += mp
+            E += e
+            N += nl
+            b.close()
+            del b
+            torch.cuda.empty_cache()
+        res["full"] = {"arrays": narrays, "lists": N, "elements": E, "waves": len(ws),
+                       "list_counts": "log-uniform [1000, 2000000]", "knobs": fknobs.__dict__,
+                       "batched_ms": round(tot_b, 2), "plain_ms": round(tot_p, 1),
+                       "speedup": round(tot_p / tot_b, 2),
+                       "batched_gbs": round(nbytes(E, N) / (tot_b * 1e-3) / 1e9, 1),
+                       "wall_s": round(time.perf_counter() - t0, 1)}
+    return res
 
 
 def measure_c5(dev, reps, warmup, n_lists=4_000_000):
@@ -737,7 +777,8 @@ def run_gb300(args):
                                                           args.lists or 10_000_000)}))
         return
     if args.only == "c4":
-        print(json.dumps({"c4_batched": measure_c4(dev, narrays=args.lists or 4096)}))
+        print(json.dumps({"c4_batched": measure_c4(dev, narrays=args.lists or 4096,
+                                                    full=not args.no_c4_full)}))
         return
     if args.only == "c5":
         print(json.dumps({"c5_autograd": measure_c5(dev, args.steps, args.warmup,
@@ -890,7 +931,7 @@ def run_gb300(args):
         line["c3_combinations"] = measure_c3(be, dev, max(args.steps // 2, 5), args.warmup)
         line["c2_jagged_slicing"] = measure_c2(be, dev, max(args.steps // 2, 5), args.warmup)
         line["c5_autograd"] = measure_c5(dev, max(args.steps // 2, 5), args.warmup)
-        line["c4_batched"] = measure_c4(dev)
+        line["c4_batched"] = measure_c4(dev, full=not args.no_c4_full)
         line["sort"] = measure_sort(be, dev, max(args.steps // 2, 5), args.warmup)
         line["nonlocal_reduce"] = measure_nonlocal(be, dev, max(args.steps // 2, 5), args.warmup)
         line["fused_reduce"] = measure_fused(be, dev, max(args.steps // 2, 5), args.warmup)
@@ -914,6 +955,8 @@ def main():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--chunks", type=int, default=8,
                    help="list chunks of the host-buffer (e2e) pipeline")
+    p.add_argument("--no-c4-full", action="store_true",
+                   help="skip the full-distribution (waves) run of the batched workload")
     p.add_argument("--no-extras", action="store_true",
                    help="skip the secondary workloads (combinations, ...)")
     p.add_argument("--only", default=None, choices=["c2", "c3", "c4", "c5", "sort", "nonlocal", "fused"],

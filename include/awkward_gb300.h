@@ -764,10 +764,14 @@ int awkward_gb300_jagged_softmax_backward_float64(double* grad_x, const double* 
  * list counts, element counts (offsets[n] - offsets[0]) and the device
  * pointers of each array's content, offsets, uint8 mask and outputs
  * (out_sum/out_max [n] float64, out_argmax/out_count [n] int64,
- * sel_offsets [n + 1] int64, sel_content [elements] float64).  Reducer
- * results are bit-identical to the per-array entry points.  plan_run only
+ * sel_offsets [n + 1] int64, sel_content [elements] float64).  Tuning
+ * knobs: order_mode (0 array order, 1 largest ranges first),
+ * occupancy_div (persistent CTAs per SM = occupancy / div), range_min
+ * (items per range of arrays with no list above 4096 elements, >= 512),
+ * block (threads per reducer CTA, 128 or 256).  Reducer results are
+ * bit-identical to the per-array entry points.  plan_run only
  * launches (capturable in a CUDA graph); plan_destroy frees the plan. */
-int awkward_gb300_batch_plan_create(void** plan, int64_t narrays, const int64_t* nlists, const int64_t* nelements, const int64_t* maxlen, const double* const* x, const int64_t* const* offsets, const uint8_t* const* mask, double* const* out_sum, double* const* out_max, int64_t* const* out_argmax, int64_t* const* out_count, int64_t* const* sel_offsets, double* const* sel_content, int64_t order_mode, int64_t occupancy_div, uint64_t* err_code);
+int awkward_gb300_batch_plan_create(void** plan, int64_t narrays, const int64_t* nlists, const int64_t* nelements, const int64_t* maxlen, const double* const* x, const int64_t* const* offsets, const uint8_t* const* mask, double* const* out_sum, double* const* out_max, int64_t* const* out_argmax, int64_t* const* out_count, int64_t* const* sel_offsets, double* const* sel_content, int64_t order_mode, int64_t occupancy_div, int64_t range_min, int64_t block, uint64_t* err_code);
 int awkward_gb300_batch_plan_run(void* plan, void* stream);
 int awkward_gb300_batch_plan_destroy(void* plan);
 

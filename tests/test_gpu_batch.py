@@ -43,14 +43,20 @@ def _batch():
     return batch.Batch(b.arrays[:20] + _special_arrays() + b.arrays[20:])
 
 
-@pytest.mark.parametrize("variant", [(0, 1), (1, 1), (1, 2), (0, 2)])
+def _variants():
+    from awkward_gb300 import batch
+
+    return batch.PLAN_VARIANTS
+
+
+@pytest.mark.parametrize("variant", _variants(), ids=lambda k: f"o{k.order_mode}d{k.occupancy_div}r{k.range_min}b{k.block}")
 def test_batched_graph_matches_per_array(variant):
     import torch
 
     from awkward_gb300 import batch
 
     b = _batch()
-    plan = b.plan(*variant)
+    plan = b.plan(variant)
     g = b.graph(plan)
     for _ in range(2):  # replays recompute everything from scratch
         g.replay()
@@ -68,13 +74,24 @@ def test_batched_graph_matches_per_array(variant):
     b.close()
 
 
-def test_autotune_caches_by_shape():
+def test_autotune_caches_by_shape(tmp_path, monkeypatch):
+    import json
+
     from awkward_gb300 import batch
 
+    monkeypatch.setenv(batch.CACHE_ENV, str(tmp_path / "tune.json"))
+    batch._TUNED.clear()
     b = batch.make_batch(16, seed=4, min_lists=100, max_lists=5_000)
-    v = batch.autotune(b)
-    assert v in batch.PLAN_VARIANTS
-    assert batch._TUNED[b.signature()] == v
+    v = batch.autotune(b, reps=1)
+    assert isinstance(v, batch.PlanKnobs)
+    for name, values in batch.KNOB_VALUES.items():
+        assert getattr(v, name) in values
+    stored = json.load(open(tmp_path / "tune.json"))
+    assert len(stored) == 1 and list(stored.values())[0] == {
+        "order_mode": v.order_mode, "occupancy_div": v.occupancy_div,
+        "range_min": v.range_min, "block": v.block}
+    assert batch.autotune(b) == v
+    batch._TUNED.clear()  # a new process: the file answers without timing
     assert batch.autotune(b) == v
     b.close()
     assert math.isfinite(batch.time_plain(b))
