@@ -25,7 +25,9 @@ device and context), so make it before any stream capture there."""
 _AUTOGRAD_COMMENT = """backward kernels of differentiable jagged operations (torch.autograd
 in awkward_gb300/autograd.py).  No counterpart in awkward, which has no
 CUDA backward kernels.  Pointers are device pointers; offsets are int64
-[nlists + 1] (need not start at 0); element arrays are indexed globally.
+[nlists + 1] (need not start at 0); element arrays are indexed globally;
+nvalues is the length of the element arrays: elements no list covers are
+set to 0, the others written by the kernels (no prior clearing needed).
   segment_sum_backward:   grad_x[j] = grad_out[list of j]
   segment_max_backward:   grad_x = 0; grad_x[argmax[l]] = grad_out[l] for
                           argmax[l] in [0, nelements) (global indices, -1 empty)
@@ -47,17 +49,17 @@ EXTENSIONS = {
 for _suffix, _t in (("float32", "float"), ("float64", "double")):
     EXTENSIONS[f"awkward_gb300_segment_sum_backward_{_suffix}"] = (
         [(f"{_t}*", "grad_x"), (f"const {_t}*", "grad_out"), ("const int64_t*", "offsets"),
-         ("int64_t", "nlists"), ("void*", "stream")], "autograd")
+         ("int64_t", "nlists"), ("int64_t", "nvalues"), ("void*", "stream")], "autograd")
     EXTENSIONS[f"awkward_gb300_segment_max_backward_{_suffix}"] = (
         [(f"{_t}*", "grad_x"), (f"const {_t}*", "grad_out"), ("const int64_t*", "argmax"),
          ("int64_t", "nelements"), ("int64_t", "nlists"), ("void*", "stream")], "autograd")
     EXTENSIONS[f"awkward_gb300_jagged_softmax_forward_{_suffix}"] = (
         [(f"{_t}*", "y"), (f"const {_t}*", "x"), ("const int64_t*", "offsets"),
-         ("int64_t", "nlists"), ("void*", "stream")], "autograd")
+         ("int64_t", "nlists"), ("int64_t", "nvalues"), ("void*", "stream")], "autograd")
     EXTENSIONS[f"awkward_gb300_jagged_softmax_backward_{_suffix}"] = (
         [(f"{_t}*", "grad_x"), (f"const {_t}*", "grad_y"), (f"const {_t}*", "x"),
          (f"const {_t}*", "y_saved"), ("const int64_t*", "offsets"), ("int64_t", "nlists"),
-         ("void*", "stream")], "autograd")
+         ("int64_t", "nvalues"), ("void*", "stream")], "autograd")
 
 _JAGGED_COMMENT = """jagged getitem steps that awkward performs with cupy array operations
 instead of kernels of its specification (no counterpart in

@@ -79,9 +79,9 @@ class SegmentSum(torch.autograd.Function):
     def backward(ctx, grad_out):
         (offsets,) = ctx.saved_tensors
         g = grad_out.contiguous()
-        gx = torch.zeros(ctx.nvalues, dtype=g.dtype, device=g.device)
+        gx = torch.empty(ctx.nvalues, dtype=g.dtype, device=g.device)  # every element written
         _launch(f"awkward_gb300_segment_sum_backward_{_SUFFIX[g.dtype]}", gx.data_ptr(),
-                g.data_ptr(), offsets.data_ptr(), offsets.numel() - 1, _stream(g))
+                g.data_ptr(), offsets.data_ptr(), offsets.numel() - 1, ctx.nvalues, _stream(g))
         return gx, None
 
 
@@ -113,9 +113,9 @@ class JaggedSoftmax(torch.autograd.Function):
     def forward(ctx, values, offsets, activation_budget=DEFAULT_ACTIVATION_BUDGET):
         _check(values, offsets)
         n = offsets.numel() - 1
-        y = torch.zeros_like(values)  # elements outside the offsets' span stay 0
+        y = torch.empty_like(values)  # elements outside the offsets' span are set to 0
         _launch(f"awkward_gb300_jagged_softmax_forward_{_SUFFIX[values.dtype]}", y.data_ptr(),
-                values.data_ptr(), offsets.data_ptr(), n, _stream(values))
+                values.data_ptr(), offsets.data_ptr(), n, values.numel(), _stream(values))
         itemsize = values.element_size()
         keep_y = (values.numel() + 2 * n) * itemsize <= activation_budget
         ctx.keep_y = keep_y
@@ -131,10 +131,10 @@ class JaggedSoftmax(torch.autograd.Function):
         values, offsets = saved[0], saved[1]
         y = saved[2] if ctx.keep_y else None
         g = grad_y.contiguous()
-        gx = torch.zeros_like(values)
+        gx = torch.empty_like(values)  # every element written (0 outside the lists)
         _launch(f"awkward_gb300_jagged_softmax_backward_{_SUFFIX[g.dtype]}", gx.data_ptr(),
                 g.data_ptr(), values.data_ptr(), y.data_ptr() if y is not None else None,
-                offsets.data_ptr(), offsets.numel() - 1, _stream(g))
+                offsets.data_ptr(), offsets.numel() - 1, values.numel(), _stream(g))
         return gx, None, None
 
 

@@ -256,16 +256,43 @@ __global__ void __launch_bounds__(kSoftThreads)
   }
 }
 
+// Zero a[j] for j outside [offsets[0], offsets[nlists]) within [0, nvalues):
+// the elements no list covers, which the kernels above never write.  Only
+// those elements are touched (none when the offsets span the whole array),
+// so the callers need not clear the whole output first.
+template <class T>
+__global__ void zero_outside_kernel(T* __restrict__ a, const int64_t* __restrict__ offsets,
+                                    long long nlists, long long nvalues) {
+  long long lo = __ldg(offsets), hi = __ldg(offsets + nlists);
+  lo = lo < 0 ? 0 : (lo > nvalues ? nvalues : lo);
+  hi = hi < lo ? lo : (hi > nvalues ? nvalues : hi);
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  for (long long j = t; j < lo; j += stride) a[j] = T(0);
+  for (long long j = hi + t; j < nvalues; j += stride) a[j] = T(0);
+}
+
+template <class T>
+cudaError_t zero_outside(T* a, const int64_t* offsets, long long nlists, long long nvalues,
+                         cudaStream_t s) {
+  if (nvalues <= 0) return cudaSuccess;
+  zero_outside_kernel<T><<<device_sm_count() * 4, 256, 0, s>>>(a, offsets, nlists, nvalues);
+  return cudaGetLastError();
+}
+
 }  // namespace
 
 // ================================================================== entry points
 #define GB_AUTOGRAD(SUFFIX, T)                                                                  \
   GB_EXPORT int awkward_gb300_segment_sum_backward_##SUFFIX(                                    \
-      T* grad_x, const T* grad_out, const int64_t* offsets, int64_t nlists, void* stream) {    \
-    if (nlists <= 0) return 0;                                                                  \
-    sum_backward_kernel<T><<<soft_tiles(nlists), kSoftThreads, 0, (cudaStream_t)stream>>>(         \
-        grad_x, grad_out, offsets, nlists);                                                     \
-    return (int)cudaGetLastError();                                                             \
+      T* grad_x, const T* grad_out, const int64_t* offsets, int64_t nlists, int64_t nvalues,   \
+      void* stream) {                                                                           \
+    cudaStream_t s = (cudaStream_t)stream;                                                      \
+    if (nlists <= 0) return (int)(nvalues > 0 ? cudaMemsetAsync(grad_x, 0, sizeof(T) * (size_t)nvalues, s) : cudaSuccess); \
+    sum_backward_kernel<T><<<soft_tiles(nlists), kSoftThreads, 0, s>>>(grad_x, grad_out,       \
+                                                                      offsets, nlists);         \
+    cudaError_t e = cudaGetLastError();                                                         \
+    return (int)(e != cudaSuccess ? e : zero_outside(grad_x, offsets, nlists, nvalues, s));     \
   }                                                                                             \
   GB_EXPORT int awkward_gb300_segment_max_backward_##SUFFIX(                                    \
       T* grad_x, const T* grad_out, const int64_t* argmax, int64_t nelements, int64_t nlists,  \
@@ -283,19 +310,22 @@ __global__ void __launch_bounds__(kSoftThreads)
     return (int)cudaGetLastError();                                                             \
   }                                                                                             \
   GB_EXPORT int awkward_gb300_jagged_softmax_forward_##SUFFIX(                                  \
-      T* y, const T* x, const int64_t* offsets, int64_t nlists, void* stream) {                \
-    if (nlists <= 0) return 0;                                                                  \
-    softmax_forward_kernel<T><<<soft_tiles(nlists), kSoftThreads, 0, (cudaStream_t)stream>>>(      \
-        y, x, offsets, nlists);                                                                 \
-    return (int)cudaGetLastError();                                                             \
+      T* y, const T* x, const int64_t* offsets, int64_t nlists, int64_t nvalues, void* stream) { \
+    cudaStream_t s = (cudaStream_t)stream;                                                      \
+    if (nlists <= 0) return (int)(nvalues > 0 ? cudaMemsetAsync(y, 0, sizeof(T) * (size_t)nvalues, s) : cudaSuccess); \
+    softmax_forward_kernel<T><<<soft_tiles(nlists), kSoftThreads, 0, s>>>(y, x, offsets, nlists); \
+    cudaError_t e = cudaGetLastError();                                                         \
+    return (int)(e != cudaSuccess ? e : zero_outside(y, offsets, nlists, nvalues, s));          \
   }                                                                                             \
   GB_EXPORT int awkward_gb300_jagged_softmax_backward_##SUFFIX(                                 \
       T* grad_x, const T* grad_y, const T* x, const T* y_saved, const int64_t* offsets,        \
-      int64_t nlists, void* stream) {                                                           \
-    if (nlists <= 0) return 0;                                                                  \
-    softmax_backward_kernel<T><<<soft_tiles(nlists), kSoftThreads, 0, (cudaStream_t)stream>>>(     \
+      int64_t nlists, int64_t nvalues, void* stream) {                                          \
+    cudaStream_t s = (cudaStream_t)stream;                                                      \
+    if (nlists <= 0) return (int)(nvalues > 0 ? cudaMemsetAsync(grad_x, 0, sizeof(T) * (size_t)nvalues, s) : cudaSuccess); \
+    softmax_backward_kernel<T><<<soft_tiles(nlists), kSoftThreads, 0, s>>>(                    \
         grad_x, grad_y, x, y_saved, offsets, nlists);                                           \
-    return (int)cudaGetLastError();                                                             \
+    cudaError_t e = cudaGetLastError();                                                         \
+    return (int)(e != cudaSuccess ? e : zero_outside(grad_x, offsets, nlists, nvalues, s));     \
   }
 
 GB_AUTOGRAD(float32, float)

@@ -741,21 +741,23 @@ int awkward_gb300_take(void* out, const void* content, int64_t itemsize, const i
 /* ---- backward kernels of differentiable jagged operations (torch.autograd
  * in awkward_gb300/autograd.py).  No counterpart in awkward, which has no
  * CUDA backward kernels.  Pointers are device pointers; offsets are int64
- * [nlists + 1] (need not start at 0); element arrays are indexed globally.
+ * [nlists + 1] (need not start at 0); element arrays are indexed globally;
+ * nvalues is the length of the element arrays: elements no list covers are
+ * set to 0, the others written by the kernels (no prior clearing needed).
  *   segment_sum_backward:   grad_x[j] = grad_out[list of j]
  *   segment_max_backward:   grad_x = 0; grad_x[argmax[l]] = grad_out[l] for
  *                           argmax[l] in [0, nelements) (global indices, -1 empty)
  *   jagged_softmax_forward: y = exp(x - max) / sum(exp(x - max)) per list
  *   jagged_softmax_backward: grad_x = y * (grad_y - sum(grad_y * y)) per list,
  *                           y from y_saved, or recomputed from x when NULL */
-int awkward_gb300_segment_sum_backward_float32(float* grad_x, const float* grad_out, const int64_t* offsets, int64_t nlists, void* stream);
+int awkward_gb300_segment_sum_backward_float32(float* grad_x, const float* grad_out, const int64_t* offsets, int64_t nlists, int64_t nvalues, void* stream);
 int awkward_gb300_segment_max_backward_float32(float* grad_x, const float* grad_out, const int64_t* argmax, int64_t nelements, int64_t nlists, void* stream);
-int awkward_gb300_jagged_softmax_forward_float32(float* y, const float* x, const int64_t* offsets, int64_t nlists, void* stream);
-int awkward_gb300_jagged_softmax_backward_float32(float* grad_x, const float* grad_y, const float* x, const float* y_saved, const int64_t* offsets, int64_t nlists, void* stream);
-int awkward_gb300_segment_sum_backward_float64(double* grad_x, const double* grad_out, const int64_t* offsets, int64_t nlists, void* stream);
+int awkward_gb300_jagged_softmax_forward_float32(float* y, const float* x, const int64_t* offsets, int64_t nlists, int64_t nvalues, void* stream);
+int awkward_gb300_jagged_softmax_backward_float32(float* grad_x, const float* grad_y, const float* x, const float* y_saved, const int64_t* offsets, int64_t nlists, int64_t nvalues, void* stream);
+int awkward_gb300_segment_sum_backward_float64(double* grad_x, const double* grad_out, const int64_t* offsets, int64_t nlists, int64_t nvalues, void* stream);
 int awkward_gb300_segment_max_backward_float64(double* grad_x, const double* grad_out, const int64_t* argmax, int64_t nelements, int64_t nlists, void* stream);
-int awkward_gb300_jagged_softmax_forward_float64(double* y, const double* x, const int64_t* offsets, int64_t nlists, void* stream);
-int awkward_gb300_jagged_softmax_backward_float64(double* grad_x, const double* grad_y, const double* x, const double* y_saved, const int64_t* offsets, int64_t nlists, void* stream);
+int awkward_gb300_jagged_softmax_forward_float64(double* y, const double* x, const int64_t* offsets, int64_t nlists, int64_t nvalues, void* stream);
+int awkward_gb300_jagged_softmax_backward_float64(double* grad_x, const double* grad_y, const double* x, const double* y_saved, const int64_t* offsets, int64_t nlists, int64_t nvalues, void* stream);
 
 /* ---- batched execution (no counterpart in awkward): sum, max, argmax and
  * count (axis=-1) and array[mask] of many float64 ListOffsetArrays in one

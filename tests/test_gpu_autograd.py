@@ -196,3 +196,29 @@ def test_full_size_sum_and_max_backward():
     assert int(nz.sum()) <= int(nonempty.sum())
     assert torch.equal(x[nz], m[owner[nz]])
     torch.testing.assert_close(xg2.grad.sum().double(), g[nonempty].sum().double(), rtol=1e-5, atol=1e-3)
+
+
+@pytest.mark.parametrize("op", ["sum", "softmax"])
+def test_elements_outside_the_lists_get_zero_gradients(op):
+    """Outputs are allocated uninitialised; the kernels must set the elements
+    no list covers (before offsets[0] and after offsets[-1]) to 0."""
+    import torch
+
+    from awkward_gb300 import autograd as ag
+
+    n_vals = 50_000
+    garbage = torch.full((4 * n_vals,), float("nan"), device="cuda")
+    del garbage  # its memory goes back to the caching allocator, still NaN
+    L = torch.full((4000,), 10, dtype=torch.int64, device="cuda")
+    off = torch.zeros(4001, dtype=torch.int64, device="cuda")
+    torch.cumsum(L, 0, out=off[1:])
+    off += 123  # 123 leading and n_vals - 40123 trailing uncovered elements
+    x = torch.randn(n_vals, dtype=torch.float32, device="cuda").requires_grad_(True)
+    y = ag.segment_sum(x, off) if op == "sum" else ag.jagged_softmax(x, off)
+    y.backward(torch.ones_like(y))
+    inside = torch.zeros(n_vals, dtype=torch.bool, device="cuda")
+    inside[123:40123] = True
+    assert bool((x.grad[~inside] == 0).all())
+    assert bool(torch.isfinite(x.grad[inside]).all())
+    if op == "softmax":
+        assert bool((y[~inside] == 0).all())
