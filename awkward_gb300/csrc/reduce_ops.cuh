@@ -65,12 +65,16 @@ __device__ __forceinline__ bool num_better(T b, T a) {
 // acc * 2^(anchor - 1075); every addend's 53-bit significand is aligned to the
 // anchor (the largest exponent seen; bits below the anchor's unit are
 // truncated, < 1 unit each) and |acc| is kept below 2^62 by raising the anchor.
-// finalize() rounds the total to nearest-even once.  Infinities and NaNs are
-// tracked in `flags` with IEEE semantics (NaN absorbs; +inf + -inf = NaN).
+// A float64 partial `dp` (the even positions of short runs, added on the
+// FP64 unit) rides along and is added once, in float64, at the end.
+// finalize() rounds the fixed-point total to nearest-even once, then adds dp.
+// Infinities and NaNs are tracked in `flags` with IEEE semantics (NaN
+// absorbs; +inf + -inf = NaN), and in dp by the float64 addition itself.
 struct FxAcc {
   long long acc;
   int anchor;  // >= 1 (1 is the subnormal scale)
   int flags;   // 1 NaN, 2 +inf, 4 -inf
+  double dp;   // float64 partial, added last
 };
 
 __device__ __forceinline__ FxAcc fx_norm(FxAcc a) {
@@ -125,14 +129,23 @@ __device__ __forceinline__ FxAcc fx_combine(FxAcc a, FxAcc b) {
   const int sh = a.anchor - b.anchor;
   a.acc += sh >= 63 ? (b.acc >> 63) : (b.acc >> sh);
   a.flags |= b.flags;
+  a.dp += b.dp;
   return fx_norm(a);
 }
 
-__device__ __forceinline__ double fx_finalize(FxAcc a) {
+// The fixed-point part acc * 2^(anchor - 1075) rounded to nearest-even.
+__device__ __forceinline__ double fx_fixed_value(FxAcc a) {
   if ((a.flags & 1) || (a.flags & 6) == 6) return __longlong_as_double(0x7ff8000000000000LL);
   if (a.flags & 2) return __longlong_as_double(0x7ff0000000000000LL);
   if (a.flags & 4) return __longlong_as_double((long long)0xfff0000000000000ULL);
   if (a.acc == 0) return 0.0;
+  if (a.anchor >= 53 && a.anchor <= 1970) {
+    // |acc| >= 1 and < 2^63: the scaled value is a normal double, so the
+    // integer's correctly rounded conversion scaled by adding to its exponent
+    // field is the rounded value (the same bits as the general path below)
+    const long long c = __double_as_longlong(__ll2double_rn(a.acc));
+    return __longlong_as_double(c + ((long long)(a.anchor - 1075) << 52));
+  }
   const unsigned long long sign = a.acc < 0 ? 0x8000000000000000ULL : 0ULL;
   unsigned long long mag = a.acc < 0 ? (unsigned long long)(-a.acc) : (unsigned long long)a.acc;
   const int p = 63 - __clzll((long long)mag);  // leading bit of mag
@@ -159,6 +172,8 @@ __device__ __forceinline__ double fx_finalize(FxAcc a) {
   return __longlong_as_double(
       (long long)(sign | ((unsigned long long)biased << 52) | (q & 0xfffffffffffffULL)));
 }
+
+__device__ __forceinline__ double fx_finalize(FxAcc a) { return fx_fixed_value(a) + a.dp; }
 
 // Sum of float64 (or float32) into float64 on the integer pipe in fixed
 // point, rounded once at the end (runs of at most 32 elements also add half
@@ -532,10 +547,10 @@ __device__ __forceinline__ FxAcc run_short(const FixedSumOp<IN>& op, const IN* p
     return a;
   } else {
     // Even positions are added in float64 (one DADD per pair, on the FP64
-    // unit, which otherwise idles) while odd positions go through the exact
-    // fixed point on the integer pipes; the double partial joins the fixed
-    // point once (fx_add_f64 also carries its inf/NaN).  The result stays
-    // within n*eps*sum|x| of the exact sum.
+    // unit) while odd positions go through the fixed point on the integer
+    // pipes; the float64 partial rides in FxAcc::dp and is added to the
+    // rounded fixed-point part at the end (IEEE inf/NaN included).  The
+    // result stays within n*eps*sum|x| of the exact sum.
     if constexpr (Ld::kTouch) touch_run(p, n, 8);
     const long long* q = reinterpret_cast<const long long*>(p);
     const int* qh = reinterpret_cast<const int*>(p) + 1;
@@ -550,7 +565,7 @@ __device__ __forceinline__ FxAcc run_short(const FixedSumOp<IN>& op, const IN* p
     }
     if (i < n) dsum += ld(p + i);
     const int half = n >> 1;  // odd positions 1, 3, ..., 2*half-1
-    if (half == 0) return fx_add_f64(op.identity(), dsum);
+    if (half == 0) return FxAcc{0, 1, 0, dsum};
     const int emax_f = ebmax >> 20, emin_f = ebmin >> 20;
     long long acc = 0;
     int anchor;
@@ -571,7 +586,8 @@ __device__ __forceinline__ FxAcc run_short(const FixedSumOp<IN>& op, const IN* p
     } else if (emax_f == 0x7ff) {  // inf / NaN among them: the general accumulator
       FxAcc a = op.identity();
       for (int k = 1; k < n; k += 2) a = fx_add_f64(a, __longlong_as_double(ld(q + k)));
-      return fx_add_f64(a, dsum);
+      a.dp = dsum;
+      return a;
     } else {  // zeros, subnormals or a wide exponent spread
       anchor = emax_f > 1 ? emax_f : 1;
       for (int k = 1; k < n; k += 2) {
@@ -584,7 +600,7 @@ __device__ __forceinline__ FxAcc run_short(const FixedSumOp<IN>& op, const IN* p
         acc += (t ^ sg) - sg;
       }
     }
-    return fx_add_f64(FxAcc{acc, anchor, 0}, dsum);
+    return FxAcc{acc, anchor, 0, dsum};
   }
 }
 
