@@ -246,7 +246,7 @@ __device__ __forceinline__ void fill_successors(long long* __restrict__ sw,
 }
 
 template <class C>
-__global__ void __launch_bounds__(kTileBlock)
+__global__ void __launch_bounds__(kTileBlock, 4)  // 64 registers: 32 warps per SM
     combinations_kernel(int64_t** __restrict__ tocarry, int64_t* __restrict__ toindex,
                         long long n, bool replacement, const C* __restrict__ starts,
                         const C* __restrict__ stops, long long length, long long ntiles,
