@@ -93,10 +93,7 @@ __global__ void __launch_bounds__(BLOCK, kSegMinBlocks * kSegBlock / BLOCK)
     const int Weff = A.ranges[K];
     const long long d0 = D * it.y / Weff, d1 = D * (it.y + 1) / Weff;
     typename Op::Out* out = out_of<K>(A);
-    seg_reduce_range(
-        op, A.x, A.offsets, A.nlists, e0, A.E, d0, d1,
-        [&](long long li, const typename Op::Acc& a) { out[li] = op.finalize(a, li); },
-        records[id]);
+    seg_reduce_range(op, A.x, A.offsets, A.nlists, e0, A.E, d0, d1, out, records[id]);
     if (lane == 0) records[id].pad = it.x;
   }
 }

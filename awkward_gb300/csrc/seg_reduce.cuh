@@ -233,89 +233,34 @@ __device__ __forceinline__ void seg_range_records(const Op& op,
   if (!tail) rec.tail_acc = op.identity();
 }
 
-// Reduce the lists of merge-path diagonal range [d0, d1) of one array
-// (whole warp).  emit(list, acc) delivers each list reduced entirely here;
-// the partials of lists crossing the range ends go to `rec`.
-template <class Op, class Emit>
-__device__ __forceinline__ void seg_reduce_range(const Op& op,
-                                                 const store_t<typename Op::In>* __restrict__ x,
-                                                 const int64_t* __restrict__ offsets,
-                                                 long long nlists, long long e0, long long E,
-                                                 long long d0, long long d1, Emit emit,
-                                                 RangeRecord<typename Op::Acc>& rec) {
-  const int lane = threadIdx.x & 31;
-  // both ends at once: lanes 0-15 search d0, lanes 16-31 search d1
-  const bool upper = lane >= 16;
-  const long long split = mp_search_half(offsets, nlists, e0, E, upper ? d1 : d0,
-                                         upper ? 0xffff0000u : 0x0000ffffu);
-  const long long I0 = __shfl_sync(0xffffffffu, split, 0);
-  const long long I1 = __shfl_sync(0xffffffffu, split, 16);
-  const long long J0 = e0 + (d0 - I0), J1 = e0 + (d1 - I1);
-  const long long last_list = I1 < nlists ? I1 : I1 - 1;  // I1 itself is the tail, if any
-
-  for (long long base = I0; base <= last_list; base += 32) {
-    const long long li = base + lane;
-    const bool act = li <= last_list;
-    long long st = 0, en = 0;
-    if (act) {
-      st = __ldg(offsets + li);
-      en = __ldg(offsets + li + 1);
-    }
-    if (li + 32 <= last_list) {  // the next round's offsets in flight (result never read)
-      long long dd;
-      asm volatile("ld.global.nc.b64 %0, [%1];" : "=l"(dd) : "l"(offsets + li + 32));
-    }
-    seg_direct_lists(op, x, base, act, st, en, I1, J0, J1, emit, rec);
-  }
-  if (lane == 0) seg_range_records(op, offsets, nlists, I0, I1, J0, rec);
-}
-
-// Number of warp ranges an array of nlists lists and E elements is split
-// into when W warps are available (the batched path uses the same split, so
-// both give bit-identical results).
-__host__ __device__ __forceinline__ int seg_ranges_min(long long nlists, long long E, int W,
-                                                       long long min_items) {
-  const long long D = nlists + E;
-  const long long wanted = (D + min_items - 1) / min_items;
-  return (int)(wanted < W ? wanted : W);
-}
-__host__ __device__ __forceinline__ int seg_ranges(long long nlists, long long E, int W) {
-  return seg_ranges_min(nlists, E, W, kMinRangeItems);
-}
-
 // The reducers with a direct finisher for a whole list of at most
 // kShortList elements (lane_final, defined with them in reduce_ops.cuh).
 template <class Op>
 struct LaneFinal : std::false_type {};
 
-// The per-array kernel.  A warp walks its merge-path range 32 lists per
-// round, one lane per list.  The lanes' list ends are one coalesced 8-byte
-// load per round (starts come from the lane below), and a round whose lists
-// all end inside the range with at most kShortList elements each -- nearly
-// every round of short-list data -- is finished by the lanes alone: each
-// computes its list's output with the reducer's short-run arithmetic
-// (lane_final where the reducer has one, else finalize(run_short)) and
-// stores it.  Other rounds (a list longer than kShortList, the giant list
-// crossing the range start, the list open at its end) take the general
-// per-round path.  Both give the same bits for a list.
+// Reduce the lists of merge-path diagonal range [d0, d1) of one array (whole
+// warp), writing each list that ends in the range to out[list]; the partials
+// of the giant lists crossing the range ends go to `rec`.
+//
+// The warp walks the range 32 lists per round, one lane per list.  The lanes'
+// list ends are one coalesced 8-byte load per round (starts come from the lane
+// below).  A round whose lists all end inside the range with at most
+// kShortList elements each -- nearly every round of short-list data -- is
+// finished by the lanes alone: each computes its list's output with the
+// reducer's short-run arithmetic (lane_final where the reducer has one, else
+// finalize(run_short)) and stores it.  Other rounds (a list longer than
+// kShortList, the giant list crossing the range start, the list open at its
+// end) take seg_direct_lists.  Both give the same bits for a list, so the
+// per-array kernel and the batched one (which both call this) agree bit for bit.
 template <class Op>
-__global__ void __launch_bounds__(kSegBlock, kSegMinBlocks)
-    seg_reduce_kernel(Op op, const store_t<typename Op::In>* __restrict__ x,
-                      const int64_t* __restrict__ offsets, long long nlists,
-                      typename Op::Out* __restrict__ out, RangeRecord<typename Op::Acc>* records,
-                      int W, uint64_t inv, uint64_t* err) {
-  (void)inv;
-  (void)err;
+__device__ __forceinline__ void seg_reduce_range(const Op& op,
+                                                 const store_t<typename Op::In>* __restrict__ x,
+                                                 const int64_t* __restrict__ offsets,
+                                                 long long nlists, long long e0, long long E,
+                                                 long long d0, long long d1,
+                                                 typename Op::Out* __restrict__ out,
+                                                 RangeRecord<typename Op::Acc>& rec) {
   const int lane = threadIdx.x & 31;
-  const int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
-  const long long e0 = __ldg(offsets);
-  const long long eN = __ldg(offsets + nlists);
-  const long long E = eN > e0 ? eN - e0 : 0;
-  const long long D = nlists + E;
-  const int Weff = seg_ranges(nlists, E, W);
-  if (w >= Weff) return;
-  const long long d0 = D * w / Weff, d1 = D * (w + 1) / Weff;
-  RangeRecord<typename Op::Acc>& rec = records[w];
   auto emit = [&](long long li, const typename Op::Acc& a) { out[li] = op.finalize(a, li); };
   // both ends at once: lanes 0-15 search d0, lanes 16-31 search d1
   const bool upper = lane >= 16;
@@ -351,6 +296,40 @@ __global__ void __launch_bounds__(kSegBlock, kSegMinBlocks)
     }
   }
   if (lane == 0) seg_range_records(op, offsets, nlists, I0, I1, J0, rec);
+}
+
+// Number of warp ranges an array of nlists lists and E elements is split
+// into when W warps are available (the batched path uses the same split, so
+// both give bit-identical results).
+__host__ __device__ __forceinline__ int seg_ranges_min(long long nlists, long long E, int W,
+                                                       long long min_items) {
+  const long long D = nlists + E;
+  const long long wanted = (D + min_items - 1) / min_items;
+  return (int)(wanted < W ? wanted : W);
+}
+__host__ __device__ __forceinline__ int seg_ranges(long long nlists, long long E, int W) {
+  return seg_ranges_min(nlists, E, W, kMinRangeItems);
+}
+
+// The per-array kernel: a persistent grid of warps, each reducing one
+// merge-path range (seg_reduce_range).
+template <class Op>
+__global__ void __launch_bounds__(kSegBlock, kSegMinBlocks)
+    seg_reduce_kernel(Op op, const store_t<typename Op::In>* __restrict__ x,
+                      const int64_t* __restrict__ offsets, long long nlists,
+                      typename Op::Out* __restrict__ out, RangeRecord<typename Op::Acc>* records,
+                      int W, uint64_t inv, uint64_t* err) {
+  (void)inv;
+  (void)err;
+  const int w = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+  const long long e0 = __ldg(offsets);
+  const long long eN = __ldg(offsets + nlists);
+  const long long E = eN > e0 ? eN - e0 : 0;
+  const long long D = nlists + E;
+  const int Weff = seg_ranges(nlists, E, W);
+  if (w >= Weff) return;
+  const long long d0 = D * w / Weff, d1 = D * (w + 1) / Weff;
+  seg_reduce_range(op, x, offsets, nlists, e0, E, d0, d1, out, records[w]);
 }
 
 // Giant lists (more than kAbsorb elements) that cross warp ranges: one warp
