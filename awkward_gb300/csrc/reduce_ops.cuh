@@ -570,18 +570,26 @@ __device__ __forceinline__ FxAcc run_short(const FixedSumOp<IN>& op, const IN* p
     long long acc = 0;
     int anchor;
     if (emax_f != 0x7ff && emin_f != 0 && emax_f - emin_f < 32) {
-      // every odd element normal and within 32 binades: two funnel shifts each
+      // every odd element normal and within 32 binades: two funnel shifts
+      // each.  The shifts take d mod 32 (wrap), and (hi >> 20) differs from
+      // the exponent only in bit 11 (the sign), so d needs no mask; a
+      // negative addend is added as its one's complement and the count of
+      // negatives added back once.
+      long long xs = 0;
+      int negs = 0;
       for (int k = 1; k < n; k += 2) {
         const long long b = ld(q + k);
         const unsigned hi = (unsigned)((unsigned long long)b >> 32);
-        const unsigned d = (unsigned)(emax_f - (int)((hi >> 20) & 0x7ff));
+        const unsigned d = (unsigned)emax_f - (hi >> 20);
         const unsigned mh = (hi & 0xfffffu) | 0x100000u;
         const unsigned tl = __funnelshift_r((unsigned)b, mh, d);
-        const unsigned th = mh >> d;
+        const unsigned th = __funnelshift_r(mh, 0u, d);
         const long long t = (long long)(((unsigned long long)th << 32) | tl);
-        const long long sg = b >> 63;
-        acc += (t ^ sg) - sg;
+        const int sg = (int)hi >> 31;  // 0 or -1
+        xs += t ^ (long long)sg;
+        negs -= sg;
       }
+      acc = xs + negs;
       anchor = emax_f;
     } else if (emax_f == 0x7ff) {  // inf / NaN among them: the general accumulator
       FxAcc a = op.identity();
