@@ -134,16 +134,46 @@ inline unsigned soft_tiles(long long nlists) {
 }
 
 // ---------------------------------------------------------------- sum backward
+// Warp rounds of 32 lists (one lane per list, list ends loaded coalesced,
+// starts from the lane below): each lane writes its list's gradient value
+// over its elements in a per-warp stage in shared memory, then the warp copies
+// the round's span out with consecutive lanes on consecutive elements
+// (coalesced stores).  A round whose span exceeds the stage (long lists)
+// writes straight from its lanes.  No block barriers: warps run independently.
+constexpr int kBcastStage = 1024;  // elements staged per warp and round
+
 template <class T>
-__global__ void __launch_bounds__(kSoftThreads)
-    sum_backward_kernel(T* __restrict__ gx, const T* __restrict__ gout,
-                        const int64_t* __restrict__ offsets, long long nlists) {
-  __shared__ SoftTile t;
-  const long long l0 = (long long)blockIdx.x * kSoftLists;
-  stage_soft_tile(t, offsets, l0, nlists, kSoftElems);
-  const long long total = t.loc[t.count];
-  for (long long q = threadIdx.x; q < total; q += blockDim.x)
-    gx[t.base + q] = __ldg(gout + l0 + soft_list(t, q));
+__global__ void __launch_bounds__(256)
+    sum_backward_rounds_kernel(T* __restrict__ gx, const T* __restrict__ gout,
+                               const int64_t* __restrict__ offsets, long long nlists) {
+  __shared__ T stage[256 / 32][kBcastStage];
+  T* sw = stage[threadIdx.x >> 5];
+  const int lane = threadIdx.x & 31;
+  const long long nrounds = (nlists + 31) / 32;
+  const long long stride = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long r = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5; r < nrounds;
+       r += stride) {
+    const long long base = r * 32, li = base + lane;
+    const bool act = li < nlists;
+    const long long en = __ldg(offsets + (act ? li : nlists - 1) + 1);
+    long long st = __shfl_up_sync(0xffffffffu, en, 1);
+    if (lane == 0) st = __ldg(offsets + base);
+    const unsigned acts = __ballot_sync(0xffffffffu, act);
+    const long long lo = __shfl_sync(0xffffffffu, st, 0);
+    const long long hi = __shfl_sync(0xffffffffu, en, 31 - __clz(acts));
+    const T g = act ? __ldg(gout + li) : T(0);
+    const bool sorted = __all_sync(0xffffffffu, !act || st <= en);
+    if (sorted && hi - lo <= kBcastStage) {
+      if (act)
+        for (long long j = st; j < en; j++) sw[j - lo] = g;
+      __syncwarp();
+      const int span = (int)(hi - lo);
+      for (int j = lane; j < span; j += 32) gx[lo + j] = sw[j];
+      __syncwarp();
+    } else if (act) {
+      for (long long j = st; j < en; j++) gx[j] = g;
+    }
+  }
 }
 
 // ---------------------------------------------------------------- max backward
@@ -289,8 +319,8 @@ cudaError_t zero_outside(T* a, const int64_t* offsets, long long nlists, long lo
       void* stream) {                                                                           \
     cudaStream_t s = (cudaStream_t)stream;                                                      \
     if (nlists <= 0) return (int)(nvalues > 0 ? cudaMemsetAsync(grad_x, 0, sizeof(T) * (size_t)nvalues, s) : cudaSuccess); \
-    sum_backward_kernel<T><<<soft_tiles(nlists), kSoftThreads, 0, s>>>(grad_x, grad_out,       \
-                                                                      offsets, nlists);         \
+    sum_backward_rounds_kernel<T><<<device_sm_count() * 8, 256, 0, s>>>(grad_x, grad_out,    \
+                                                                       offsets, nlists);        \
     cudaError_t e = cudaGetLastError();                                                         \
     return (int)(e != cudaSuccess ? e : zero_outside(grad_x, offsets, nlists, nvalues, s));     \
   }                                                                                             \
