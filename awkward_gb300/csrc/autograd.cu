@@ -216,12 +216,12 @@ __global__ void __launch_bounds__(kSoftThreads)
     T sum = 0;
     for (long long q = a; q < b; q++) sum += exp_t(xs[q] - m);
     s_max[r] = m;
-    s_sum[r] = sum;
+    s_sum[r] = T(1) / sum;  // one division per list; elements multiply by it
   }
   __syncthreads();
   for (long long q = threadIdx.x; q < total; q += blockDim.x) {
     const int l = soft_list(t, q);
-    y[t.base + q] = exp_t(xs[q] - s_max[l]) / s_sum[l];
+    y[t.base + q] = exp_t(xs[q] - s_max[l]) * s_sum[l];
   }
 }
 
@@ -275,13 +275,14 @@ __global__ void __launch_bounds__(kSoftThreads)
       gsum += gs[q] * e;
     }
     s_max[r] = m;
-    s_sum[r] = sum;
-    s_dot[r] = gsum / sum;
+    const T inv = T(1) / sum;  // one division per list; elements multiply by it
+    s_sum[r] = inv;
+    s_dot[r] = gsum * inv;
   }
   __syncthreads();
   for (long long q = threadIdx.x; q < total; q += blockDim.x) {
     const int l = soft_list(t, q);
-    const T yj = exp_t(as[q] - s_max[l]) / s_sum[l];
+    const T yj = exp_t(as[q] - s_max[l]) * s_sum[l];
     gx[t.base + q] = yj * (gs[q] - s_dot[l]);
   }
 }
