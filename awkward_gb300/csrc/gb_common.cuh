@@ -8,8 +8,6 @@
 //    carries), never handed to the caller;
 //  * warp / block scans and reductions over arbitrary (trivially copyable)
 //    value types with an ordered, possibly non-commutative combine;
-//  * 1-D TMA bulk copies global -> shared (cp.async.bulk + mbarrier) with
-//    bounded waits;
 //  * a decoupled look-back over int64 tile aggregates with bounded spins.
 #pragma once
 
@@ -113,54 +111,6 @@ __device__ __forceinline__ V block_exclusive_scan(V v, Op op, V identity, V* sme
   *total = smem[NW];
   __syncthreads();
   return excl;
-}
-
-// ----------------------------------------------------------------- TMA bulk
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
-}
-__device__ __forceinline__ void fence_barrier_init() {
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-// Order this thread's earlier generic-proxy shared-memory accesses before
-// later async-proxy (TMA) writes to the same memory.
-__device__ __forceinline__ void fence_proxy_async_smem() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
-}
-// 1-D bulk copy global -> shared completing on `bar`.  Requirements (checked
-// by the callers): both addresses 16-byte aligned, bytes a multiple of 16.
-__device__ __forceinline__ void bulk_g2s(void* sdst, const void* gsrc, uint32_t bytes,
-                                         uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-          smem_u32(sdst)),
-      "l"(gsrc), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
-// Bounded wait for phase `parity` of `bar`.  Returns false if it gave up.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, uint32_t max_iter) {
-  uint32_t done = 0;
-  for (uint32_t it = 0; it < max_iter; it++) {
-    asm volatile(
-        "{\n"
-        ".reg .pred p;\n"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
-        "selp.u32 %0, 1, 0, p;\n"
-        "}\n"
-        : "=r"(done)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
 }
 
 // ----------------------------------------------------------------- look-back
