@@ -67,6 +67,8 @@ constexpr int kShortList = 32;        // longest list reduced by one lane
 constexpr int kMediumList = 256;      // longest list reduced by a group of 8 lanes
 constexpr int kMinRangeItems = 512;   // smallest merge range given to a warp
 constexpr long long kAbsorb = 4096;   // longest list reduced whole by the range where it ends
+constexpr int kPrefetchLines = 16;    // 128-byte lines after each round prefetched towards L2
+constexpr int kPrefetchSkip = 0;      // lines skipped before the prefetched ones
 
 // Merge-path split of diagonal d in global memory by a half warp (16 lanes,
 // `mask` selects them).  Returns the number of list ends among the first d
@@ -278,6 +280,14 @@ __device__ __forceinline__ void seg_reduce_range(const Op& op,
     long long st = __shfl_up_sync(0xffffffffu, en, 1);
     if (lane == 0) st = carry;
     carry = __shfl_sync(0xffffffffu, en, 31);
+    if (kPrefetchLines > 0 && base + 32 <= last_list && lane < kPrefetchLines) {
+      // the content after this round (the next round's, contiguous) towards
+      // L2: one 128-byte line per lane, kPrefetchSkip lines ahead, never past
+      // the array's last element
+      const long long ahead = (long long)(lane + kPrefetchSkip) * 128 / (long long)sizeof(*x);
+      if (carry + ahead < e0 + E)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(x + carry + ahead));
+    }
     const long long n = en - st;
     // every list of the round whole, short and ending in the range (I1 is
     // the list open at the range end)
