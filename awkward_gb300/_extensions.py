@@ -68,6 +68,9 @@ kernel-specification.yml):
     indexed globally over offsets[0]..offsets[nlists]) -> new offsets
     [nlists + 1] and, for each true entry in order, its position within its
     list (src/awkward/_slicing.py:476-530: localindex + compaction + cumsum);
+  jagged_mask_select: array[mask] in one pass -- the new offsets, the
+    selected content (itemsize 1, 2, 4 or 8) and optionally the carry
+    (NULL to skip), without the local index of the chain;
   take: out[i] = content[carry[i]] for itemsize 1, 2, 4 or 8 bytes
     (NumpyArray._carry); a carry outside [0, contentlen) sets err_code to
     invocation_index*256 + 0 ("index out of range")."""
@@ -75,6 +78,11 @@ kernel-specification.yml):
 EXTENSIONS["awkward_gb300_jagged_mask_to_index"] = (
     [("int64_t*", "tooffsets"), ("int64_t*", "toindex"), ("const uint8_t*", "mask"),
      ("const int64_t*", "offsets"), ("int64_t", "nlists"), ("uint64_t*", "err_code"),
+     ("void*", "stream")], "jagged")
+EXTENSIONS["awkward_gb300_jagged_mask_select"] = (
+    [("int64_t*", "tooffsets"), ("void*", "tocontent"), ("int64_t*", "tocarry"),
+     ("const uint8_t*", "mask"), ("const int64_t*", "offsets"), ("const void*", "content"),
+     ("int64_t", "itemsize"), ("int64_t", "nlists"), ("uint64_t*", "err_code"),
      ("void*", "stream")], "jagged")
 EXTENSIONS["awkward_gb300_take"] = (
     [("void*", "out"), ("const void*", "content"), ("int64_t", "itemsize"),

@@ -222,6 +222,112 @@ __global__ void take_kernel(W* __restrict__ out, const W* __restrict__ content,
   }
 }
 
+// array[mask] in one pass: per tile of kTileLists lists, the counts of true
+// mask bytes per list (popcounts of the tile's mask staged as a bitmap in
+// shared memory when it fits kMaskBits, else thread-per-list byte loops) are
+// scanned across tiles (decoupled look-back) into the new offsets; then each
+// warp walks a contiguous share of the tile's elements 32 at a time, ranks
+// the true entries with a ballot prefix and writes each selected element
+// (and, when asked, its carry: its position in the content) at its rank.  The local index and the carry of
+// the three-step chain are never materialised.
+template <class W>
+__global__ void __launch_bounds__(kTileBlock)
+    mask_select_kernel(int64_t* __restrict__ tooffsets, W* __restrict__ tocontent,
+                       int64_t* __restrict__ tocarry, const uint8_t* __restrict__ mask,
+                       const int64_t* __restrict__ offsets, const W* __restrict__ content,
+                       long long nlists, long long ntiles, ScanTiles st, uint64_t* err) {
+  __shared__ TileSmem sm;
+  __shared__ long long loc[kTileLists + 1];
+  __shared__ unsigned sbits[kMaskBits / 32];  // the tile's mask as a bitmap (when it fits)
+  const long long tile = tile_claim(sm, st);
+  const long long l0 = tile * kTileLists;
+  const long long rem = nlists - l0;
+  const int count = (int)(rem < kTileLists ? rem : kTileLists);
+  const long long base = __ldg(offsets + l0);
+  for (int i = threadIdx.x; i <= kTileLists; i += kTileBlock) {
+    const int k = i < count ? i : count;
+    loc[i] = __ldg(offsets + l0 + k) - base;
+  }
+  __syncthreads();
+  const long long total = loc[count];
+  const uint8_t* p0 = mask + base;
+  const int sh = (int)(reinterpret_cast<uintptr_t>(p0) & 15);
+  const bool staged = total + sh <= kMaskBits;
+  long long c[kTileLPT];
+  if (staged) {
+    // the tile's mask bytes as a bitmap (two aligned 16-byte loads per word,
+    // byte loads at the partial ends); counts are popcounts of it
+    const int nbits = (int)total + sh;
+    const uint8_t* a0 = p0 - sh;
+    for (int w = threadIdx.x; w < (nbits + 31) >> 5; w += kTileBlock) {
+      const int lo = 32 * w, hi = lo + 32;
+      unsigned word = 0;
+      if (lo >= sh && hi <= nbits) {
+        const uint4 v0 = __ldg(reinterpret_cast<const uint4*>(a0 + lo));
+        const uint4 v1 = __ldg(reinterpret_cast<const uint4*>(a0 + lo + 16));
+        word = nonzero_bits16(v0) | nonzero_bits16(v1) << 16;
+      } else {
+        const int b0 = lo > sh ? lo : sh, b1 = hi < nbits ? hi : nbits;
+        for (int b = b0; b < b1; b++) word |= (unsigned)(a0[b] != 0) << (b - lo);
+      }
+      sbits[w] = word;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < kTileLPT; r++) {
+      const int li = threadIdx.x * kTileLPT + r;
+      c[r] = li < count ? bitmap_count(sbits, (int)loc[li] + sh, (int)loc[li + 1] + sh) : 0;
+    }
+  } else {
+#pragma unroll
+    for (int r = 0; r < kTileLPT; r++) {
+      const int li = threadIdx.x * kTileLPT + r;
+      long long n = 0;
+      if (li < count)
+        for (long long j = base + loc[li]; j < base + loc[li + 1]; j++) n += __ldg(mask + j) != 0;
+      c[r] = n;
+    }
+  }
+  const long long prefix = tile_scan(sm, st, tile, c, 0, err);
+  for (int li = threadIdx.x; li < count; li += kTileBlock) tooffsets[l0 + li] = prefix + sm.loc[li];
+  if (tile == ntiles - 1 && threadIdx.x == 0) tooffsets[l0 + count] = prefix + sm.total;
+  constexpr int kWarps = kTileBlock / 32;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const long long qa = total * warp / kWarps, qb = total * (warp + 1) / kWarps;
+  if (qa >= qb) return;
+  int lo = 0, hi = count;  // the list holding element qa
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (loc[mid] <= qa) lo = mid;
+    else hi = mid;
+  }
+  long long before;  // true entries of that list before qa
+  if (staged) {
+    before = bitmap_count(sbits, (int)loc[lo] + sh, (int)qa + sh);
+  } else {
+    before = 0;
+    for (long long q = loc[lo] + lane; q < qa; q += 32) before += __ldg(mask + base + q) != 0;
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) before += __shfl_xor_sync(0xffffffffu, before, d);
+  }
+  long long run = prefix + sm.loc[lo] + before;
+  for (long long g = qa; g < qb; g += 32) {
+    const long long q = g + lane;
+    bool m = false;
+    if (q < qb) {
+      const int bq = (int)q + sh;
+      m = staged ? ((sbits[bq >> 5] >> (bq & 31)) & 1u) != 0 : __ldg(mask + base + q) != 0;
+    }
+    const unsigned b = __ballot_sync(0xffffffffu, m);
+    if (m) {
+      const long long at = run + __popc(b & ((1u << lane) - 1u));
+      tocontent[at] = __ldg(content + base + q);
+      if (tocarry) tocarry[at] = base + q;
+    }
+    run += __popc(b);
+  }
+}
+
 }  // namespace
 
 // The new offsets (nlists + 1 entries) and, for each true entry of the mask
@@ -277,4 +383,50 @@ GB_EXPORT int awkward_gb300_take(void* out, const void* content, int64_t itemsiz
       return (int)cudaErrorInvalidValue;
   }
   return (int)cudaGetLastError();
+}
+
+// array[mask] for a ListOffsetArray over content of 1, 2, 4 or 8-byte items
+// in one pass: the new offsets (nlists + 1), the selected content and, when
+// tocarry is not NULL, each selected element's position in the content (the
+// carry the three-step chain would produce).  tocontent / tocarry hold as many
+// entries as the mask has true values in the offsets' span.
+GB_EXPORT int awkward_gb300_jagged_mask_select(int64_t* tooffsets, void* tocontent,
+                                               int64_t* tocarry, const uint8_t* mask,
+                                               const int64_t* offsets, const void* content,
+                                               int64_t itemsize, int64_t nlists,
+                                               uint64_t* err_code, void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (itemsize != 1 && itemsize != 2 && itemsize != 4 && itemsize != 8)
+    return (int)cudaErrorInvalidValue;
+  if (nlists <= 0) return (int)cudaMemsetAsync(tooffsets, 0, sizeof(int64_t), s);
+  const long long nt = tile_count(nlists);
+  ScanTiles st;
+  void* scratch = nullptr;
+  cudaError_t e = scan_tiles_alloc(&st, &scratch, nt, s);
+  if (e != cudaSuccess) return (int)e;
+  const unsigned grid = (unsigned)nt;
+  switch (itemsize) {
+    case 1:
+      mask_select_kernel<uint8_t><<<grid, kTileBlock, 0, s>>>(
+          tooffsets, (uint8_t*)tocontent, tocarry, mask, offsets, (const uint8_t*)content,
+          nlists, nt, st, err_code);
+      break;
+    case 2:
+      mask_select_kernel<uint16_t><<<grid, kTileBlock, 0, s>>>(
+          tooffsets, (uint16_t*)tocontent, tocarry, mask, offsets, (const uint16_t*)content,
+          nlists, nt, st, err_code);
+      break;
+    case 4:
+      mask_select_kernel<uint32_t><<<grid, kTileBlock, 0, s>>>(
+          tooffsets, (uint32_t*)tocontent, tocarry, mask, offsets, (const uint32_t*)content,
+          nlists, nt, st, err_code);
+      break;
+    default:
+      mask_select_kernel<uint64_t><<<grid, kTileBlock, 0, s>>>(
+          tooffsets, (uint64_t*)tocontent, tocarry, mask, offsets, (const uint64_t*)content,
+          nlists, nt, st, err_code);
+  }
+  e = cudaGetLastError();
+  cudaError_t f = scratch_free(scratch, s);
+  return (int)(e != cudaSuccess ? e : f);
 }

@@ -77,6 +77,30 @@ def jagged_mask_to_index(offsets, mask):
     return tooffsets, toindex[:k]
 
 
+def mask_select(offsets, content, mask, with_carry=False):
+    """array[mask] in one pass (awkward_gb300_jagged_mask_select): the new
+    offsets, the selected content and, with `with_carry`, the carry (each
+    selected element's position in the content) -- the same outputs as
+    getitem_jagged_mask without its intermediate local index."""
+    n = offsets.numel() - 1
+    span = int(offsets[-1].item() - offsets[0].item()) if n > 0 else 0
+    tooffsets = torch.empty(n + 1, dtype=torch.int64, device=offsets.device)
+    out = torch.empty(max(span, 1), dtype=content.dtype, device=content.device)
+    carry = torch.empty(max(span, 1), dtype=torch.int64, device=offsets.device) if with_carry else None
+    m = mask.view(torch.uint8) if mask.dtype == torch.bool else mask
+    err = _err_word(offsets.device)
+    rc = _abi.ext_cfunc("awkward_gb300_jagged_mask_select")(
+        tooffsets.data_ptr(), out.data_ptr(), carry.data_ptr() if with_carry else None,
+        m.data_ptr(), offsets.data_ptr(), content.data_ptr(), content.element_size(), n,
+        err.data_ptr(), _stream(offsets))
+    if rc != 0:
+        raise RuntimeError(f"awkward_gb300_jagged_mask_select: cudaError {rc}")
+    k = int(tooffsets[-1].item()) if n > 0 else 0
+    if with_carry:
+        return tooffsets, out[:k], carry[:k]
+    return tooffsets, out[:k]
+
+
 def jagged_apply(offsets, index_offsets, index, contentlen):
     """(tooffsets, tocarry) of a jagged int index applied to lists with these offsets."""
     be = backend()

@@ -418,6 +418,14 @@ def measure_c2(be, dev, reps, warmup, n_lists=10_000_000):
         k_apply(m_too, m_carry, m_ist, m_isp, n_lists, m_idx[:Km], Km, starts, stops, E)
         f_take(m_out.data_ptr(), x.data_ptr(), 4, m_carry.data_ptr(), Km, E, 0, err.data_ptr(), sp)
 
+    f_sel = _abi.ext_cfunc("awkward_gb300_jagged_mask_select")
+    s_off = torch.empty(n_lists + 1, dtype=torch.int64, device=dev)
+    s_out = torch.empty(E, dtype=torch.float32, device=dev)
+
+    def mask_one_pass():
+        f_sel(s_off.data_ptr(), s_out.data_ptr(), None, mask.data_ptr(), off.data_ptr(),
+              x.data_ptr(), 4, n_lists, err.data_ptr(), sp)
+
     Ki = idx.numel()
     i_ist, i_isp = ioff[:-1].contiguous(), ioff[1:].contiguous()
     i_too = torch.empty(n_lists + 1, dtype=torch.int64, device=dev)
@@ -460,9 +468,12 @@ def measure_c2(be, dev, reps, warmup, n_lists=10_000_000):
         + 16 * Km,
         "index": (32 * N + 16 * Ki + 8 * (N + 1)) + 16 * Ki,
         "range": (16 * ninner + 8) + (16 * ninner + 8 * (ninner + 1) + 8 * Kr) + 16 * Kr,
+        # one pass: mask and offsets read, the content read once, new offsets and
+        # the selected content written
+        "mask_one_pass": E + 8 * (N + 1) + 4 * E + 8 * (N + 1) + 4 * Km,
     }
     for name, fn, nl in (("mask", mask_chain, N), ("index", index_chain, N),
-                         ("range", range_chain, N)):
+                         ("range", range_chain, N), ("mask_one_pass", mask_one_pass, N)):
         for _ in range(max(warmup, 3)):
             fn()
         be.synchronize()
@@ -473,6 +484,8 @@ def measure_c2(be, dev, reps, warmup, n_lists=10_000_000):
     res["mask"]["kernels"] = "mask_to_index + jagged_apply + take (float32)"
     res["index"]["kernels"] = "jagged_apply + take (float32)"
     res["range"]["kernels"] = "next_range_carrylength + next_range + take (float32)"
+    res["mask_one_pass"]["kernels"] = ("awkward_gb300_jagged_mask_select: array[mask] in one "
+                                       "kernel (same offsets and content as the chain)")
     res["sizes"] = {"lists": N, "elements": E, "selected": Km, "indices": Ki,
                     "inner_lists": ninner, "inner_elements": E2, "range_kept": Kr}
     return res

@@ -270,3 +270,31 @@ def test_full_size_chains_properties():
     assert torch.equal(nxc, torch.nonzero(keep).flatten())
     Lt = torch.from_numpy(Li).cuda()
     assert torch.equal(nxo[1:] - nxo[:-1], torch.clamp(Lt - 1, min=0))
+
+
+@pytest.mark.parametrize("variant", ["poisson", "base", "all_true", "all_false", "long_list",
+                                     "half_empty"])
+@pytest.mark.parametrize("dt", [np.uint8, np.int16, np.float32, np.float64])
+def test_one_pass_mask_select_equals_the_chain(variant, dt):
+    """array[mask] in one pass gives the chain's offsets, carry and content, bit for bit."""
+    import torch
+
+    from awkward_gb300 import jagged
+
+    p = {"all_true": 1.0, "all_false": 0.0}.get(variant, 0.4)
+    extra = np.array([100_000]) if variant == "long_list" else None
+    pe = 0.5 if variant == "half_empty" else 0.01
+    _rng, L, off, x, mask = _case(20_000, 7, base=5 if variant == "base" else 0, extra=extra,
+                                  p=p, pe=pe)
+    xs = (x * 3).astype(dt) if np.dtype(dt).kind != "f" else x.astype(dt)
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    doff, dx, dm = d(off), d(xs), d(mask)
+    so, sc, scarry = jagged.mask_select(doff, dx, dm, with_carry=True)
+    io, idx = jagged.jagged_mask_to_index(doff, dm)
+    co, ccarry = jagged.jagged_apply(doff, io, idx, dx.numel())
+    cc = jagged.take(dx, ccarry)
+    torch.testing.assert_close(so, co, rtol=0, atol=0)
+    torch.testing.assert_close(scarry, ccarry, rtol=0, atol=0)
+    assert torch.equal(sc.view(torch.uint8), cc.view(torch.uint8))
+    so2, sc2 = jagged.mask_select(doff, dx, dm)
+    assert torch.equal(so2, so) and torch.equal(sc2.view(torch.uint8), sc.view(torch.uint8))
