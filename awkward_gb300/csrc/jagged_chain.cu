@@ -311,20 +311,34 @@ __global__ void __launch_bounds__(kTileBlock)
     for (int d = 16; d > 0; d >>= 1) before += __shfl_xor_sync(0xffffffffu, before, d);
   }
   long long run = prefix + sm.loc[lo] + before;
-  for (long long g = qa; g < qb; g += 32) {
-    const long long q = g + lane;
-    bool m = false;
-    if (q < qb) {
-      const int bq = (int)q + sh;
-      m = staged ? ((sbits[bq >> 5] >> (bq & 31)) & 1u) != 0 : __ldg(mask + base + q) != 0;
+  // kWalkUnroll groups of 32 elements per step: their content loads are all
+  // issued before the ballots rank them, so a warp keeps several loads in
+  // flight instead of one per group
+  constexpr int kWalkUnroll = 4;
+  const unsigned below = (1u << lane) - 1u;
+  for (long long g = qa; g < qb; g += 32 * kWalkUnroll) {
+    bool m[kWalkUnroll];
+    W v[kWalkUnroll];
+#pragma unroll
+    for (int u = 0; u < kWalkUnroll; u++) {
+      const long long q = g + 32 * u + lane;
+      m[u] = false;
+      if (q < qb) {
+        const int bq = (int)q + sh;
+        m[u] = staged ? ((sbits[bq >> 5] >> (bq & 31)) & 1u) != 0 : __ldg(mask + base + q) != 0;
+      }
+      v[u] = m[u] ? __ldg(content + base + q) : W(0);
     }
-    const unsigned b = __ballot_sync(0xffffffffu, m);
-    if (m) {
-      const long long at = run + __popc(b & ((1u << lane) - 1u));
-      tocontent[at] = __ldg(content + base + q);
-      if (tocarry) tocarry[at] = base + q;
+#pragma unroll
+    for (int u = 0; u < kWalkUnroll; u++) {
+      const unsigned b = __ballot_sync(0xffffffffu, m[u]);
+      if (m[u]) {
+        const long long at = run + __popc(b & below);
+        tocontent[at] = v[u];
+        if (tocarry) tocarry[at] = base + g + 32 * u + lane;
+      }
+      run += __popc(b);
     }
-    run += __popc(b);
   }
 }
 
