@@ -231,7 +231,7 @@ __global__ void take_kernel(W* __restrict__ out, const W* __restrict__ content,
 // (and, when asked, its carry: its position in the content) at its rank.  The local index and the carry of
 // the three-step chain are never materialised.
 template <class W>
-__global__ void __launch_bounds__(kTileBlock)
+__global__ void __launch_bounds__(kTileBlock, 8)
     mask_select_kernel(int64_t* __restrict__ tooffsets, W* __restrict__ tocontent,
                        int64_t* __restrict__ tocarry, const uint8_t* __restrict__ mask,
                        const int64_t* __restrict__ offsets, const W* __restrict__ content,
@@ -312,10 +312,46 @@ __global__ void __launch_bounds__(kTileBlock)
   }
   long long run = prefix + sm.loc[lo] + before;
   // kWalkUnroll groups of 32 elements per step: their content loads are all
-  // issued before the ballots rank them, so a warp keeps several loads in
+  // issued before the groups are ranked, so a warp keeps several loads in
   // flight instead of one per group
   constexpr int kWalkUnroll = 4;
   const unsigned below = (1u << lane) - 1u;
+  if (staged) {
+    // the warp's bit positions [b0, b1) of the staged bitmap, one bitmap word
+    // (32 elements) per group: a lane's flag is its bit of the word and its
+    // rank the set bits below it, in 32-bit tile-local arithmetic
+    const int b0 = (int)qa + sh, b1 = (int)qb + sh;
+    const int w0 = b0 >> 5, wl = (b1 - 1) >> 5;
+    const unsigned first = ~0u << (b0 & 31);
+    const unsigned last = (b1 & 31) ? (1u << (b1 & 31)) - 1u : ~0u;
+    const W* cbase = content + base;
+    W* obase = tocontent + run;
+    int64_t* kbase = tocarry ? tocarry + run : nullptr;
+    int r = 0;
+    for (int w = w0; w <= wl; w += kWalkUnroll) {
+      unsigned bits[kWalkUnroll];
+      W v[kWalkUnroll];
+#pragma unroll
+      for (int u = 0; u < kWalkUnroll; u++) {
+        const int ww = w + u;
+        unsigned b = ww <= wl ? sbits[ww] : 0u;
+        if (ww == w0) b &= first;
+        if (ww == wl) b &= last;
+        bits[u] = b;
+        v[u] = (b >> lane) & 1u ? __ldg(cbase + (32 * ww + lane - sh)) : W(0);
+      }
+#pragma unroll
+      for (int u = 0; u < kWalkUnroll; u++) {
+        if ((bits[u] >> lane) & 1u) {
+          const int at = r + __popc(bits[u] & below);
+          obase[at] = v[u];
+          if (kbase) kbase[at] = base + (32 * (w + u) + lane - sh);
+        }
+        r += __popc(bits[u]);
+      }
+    }
+    return;
+  }
   for (long long g = qa; g < qb; g += 32 * kWalkUnroll) {
     bool m[kWalkUnroll];
     W v[kWalkUnroll];

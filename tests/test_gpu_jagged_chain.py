@@ -298,3 +298,18 @@ def test_one_pass_mask_select_equals_the_chain(variant, dt):
     assert torch.equal(sc.view(torch.uint8), cc.view(torch.uint8))
     so2, sc2 = jagged.mask_select(doff, dx, dm)
     assert torch.equal(so2, so) and torch.equal(sc2.view(torch.uint8), sc.view(torch.uint8))
+
+
+@pytest.mark.parametrize("n", [0, 1, 5000])
+def test_one_pass_mask_select_no_elements(n):
+    """No lists, or lists that are all empty: offsets of zeros and no content."""
+    import torch
+
+    from awkward_gb300 import jagged
+
+    doff = torch.zeros(n + 1, dtype=torch.int64, device="cuda")
+    dx = torch.zeros(0, dtype=torch.float32, device="cuda")
+    dm = torch.zeros(0, dtype=torch.bool, device="cuda")
+    so, sc, scarry = jagged.mask_select(doff, dx, dm, with_carry=True)
+    assert torch.equal(so, torch.zeros(n + 1, dtype=torch.int64, device="cuda"))
+    assert sc.numel() == 0 and scarry.numel() == 0
