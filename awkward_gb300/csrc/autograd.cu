@@ -10,10 +10,12 @@
 // The forward sum and max use the segmented reducers of this library.
 //
 // Layout: a CTA owns a tile of kSoftLists consecutive lists, one statistics
-// thread per list, and twice as many threads for the memory passes.  It stages the tile's offsets and, when the tile's elements fit
+// thread per list, and twice as many threads for the memory passes.  It stages
+// the tile's offsets and, when the tile's elements fit
 // (kSoftBytes per array), the element arrays it reads more than once in
-// shared memory with coalesced loads, plus an element -> list map (one byte
-// per element).  Per-list statistics (max, sums) are computed by one thread
+// shared memory by asynchronous copies (cp.async, issued from the tile's two
+// end offsets so they are in flight with the offsets loads), plus an
+// element -> list map (one byte per element).  Per-list statistics (max, sums) are computed by one thread
 // per list in element order, from shared memory; then the tile's elements are
 // visited with consecutive threads on consecutive elements, so every global
 // read and write is coalesced.  A tile whose elements do not fit reads them
@@ -36,10 +38,10 @@ __device__ __forceinline__ double exp_t<double>(double v) { return exp(v); }
 template <class T>
 __device__ __forceinline__ T max_t(T a, T b) { return a > b ? a : b; }
 
-constexpr int kSoftLists = 128;       // lists per CTA (one statistics thread each)
-constexpr int kSoftThreads = 256;     // threads per CTA (staging and element passes)
-constexpr int kSoftBytes = 16384;     // staging per element array
-constexpr int kSoftElems = 4096;      // element -> list map entries (>= kSoftBytes / 4)
+constexpr int kSoftLists = 64;        // lists per CTA (one statistics thread each)
+constexpr int kSoftThreads = 128;     // threads per CTA (staging and element passes)
+constexpr int kSoftBytes = 8192;      // staging per element array
+constexpr int kSoftElems = 2048;      // element -> list map entries (>= kSoftBytes / 4)
 
 struct SoftTile {
   long long loc[kSoftLists + 1];  // offsets of the tile's lists, relative to its first element
@@ -49,13 +51,39 @@ struct SoftTile {
   int mapped;                     // owner[] holds every element's list
 };
 
-// Stage offsets[l0 .. l0+count] and, if the tile has at most `cap` elements,
-// the element -> list map (all threads; ends with __syncthreads).
+// One element global -> shared memory without a register round trip
+// (cp.async, completed by cp_async_wait_all).
+template <class T>
+__device__ __forceinline__ void cp_async_elem(T* dst, const T* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(d), "l"(src), "n"(sizeof(T))
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+// Stage a tile: offsets[l0 .. l0+count] and, if the tile has at most `cap`
+// elements, its elements of src0 (and src1 when given) into dst0 (dst1) and
+// the element -> list map (all threads; ends with __syncthreads).  The
+// element copies are issued first, from the tile's two end offsets alone, so
+// they are in flight together with the offsets loads.
+template <class T>
 __device__ __forceinline__ void stage_soft_tile(SoftTile& t, const int64_t* __restrict__ offsets,
-                                                long long l0, long long nlists, int cap) {
+                                                long long l0, long long nlists, int cap,
+                                                T* dst0, const T* __restrict__ src0, T* dst1,
+                                                const T* __restrict__ src1) {
   const long long rem = nlists - l0;
   const int count = (int)(rem < kSoftLists ? rem : kSoftLists);
   const long long base = __ldg(offsets + l0);
+  const long long total = __ldg(offsets + l0 + count) - base;
+  const bool mapped = total <= cap;
+  if (mapped) {
+    for (long long q = threadIdx.x; q < total; q += blockDim.x) {
+      cp_async_elem(dst0 + q, src0 + base + q);
+      if (src1) cp_async_elem(dst1 + q, src1 + base + q);
+    }
+  }
   for (int i = threadIdx.x; i <= kSoftLists; i += blockDim.x) {
     const int k = i < count ? i : count;
     t.loc[i] = __ldg(offsets + l0 + k) - base;
@@ -63,14 +91,14 @@ __device__ __forceinline__ void stage_soft_tile(SoftTile& t, const int64_t* __re
   if (threadIdx.x == 0) {
     t.base = base;
     t.count = count;
+    t.mapped = mapped ? 1 : 0;
   }
   __syncthreads();
-  const bool mapped = t.loc[count] <= cap;
   if (mapped && (int)threadIdx.x < count) {
     const int a = (int)t.loc[threadIdx.x], b = (int)t.loc[threadIdx.x + 1];
     for (int q = a; q < b; q++) t.owner[q] = (unsigned char)threadIdx.x;
   }
-  if (threadIdx.x == 0) t.mapped = mapped ? 1 : 0;
+  cp_async_wait_all();
   __syncthreads();
 }
 
@@ -84,49 +112,6 @@ __device__ __forceinline__ int soft_list(const SoftTile& t, long long q) {
     else hi = mid;
   }
   return lo;
-}
-
-// Copy src[0 .. n) to dst (shared memory), four loads in flight per thread.
-template <class T>
-__device__ __forceinline__ void stage_elements(T* dst, const T* __restrict__ src, long long n) {
-  const int nb = blockDim.x;
-  for (long long q0 = threadIdx.x; q0 < n; q0 += 4ll * nb) {
-    T v[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      const long long q = q0 + (long long)k * nb;
-      v[k] = q < n ? __ldg(src + q) : T(0);
-    }
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      const long long q = q0 + (long long)k * nb;
-      if (q < n) dst[q] = v[k];
-    }
-  }
-}
-
-// The same for two arrays at once (eight loads in flight per thread).
-template <class T>
-__device__ __forceinline__ void stage_elements2(T* dst0, const T* __restrict__ src0, T* dst1,
-                                                const T* __restrict__ src1, long long n) {
-  const int nb = blockDim.x;
-  for (long long q0 = threadIdx.x; q0 < n; q0 += 4ll * nb) {
-    T v[4], w[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      const long long q = q0 + (long long)k * nb;
-      v[k] = q < n ? __ldg(src0 + q) : T(0);
-      w[k] = q < n ? __ldg(src1 + q) : T(0);
-    }
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-      const long long q = q0 + (long long)k * nb;
-      if (q < n) {
-        dst0[q] = v[k];
-        dst1[q] = w[k];
-      }
-    }
-  }
 }
 
 inline unsigned soft_tiles(long long nlists) {
@@ -201,12 +186,8 @@ __global__ void __launch_bounds__(kSoftThreads)
   __shared__ T s_max[kSoftLists];
   __shared__ T s_sum[kSoftLists];
   const long long l0 = (long long)blockIdx.x * kSoftLists;
-  stage_soft_tile(t, offsets, l0, nlists, cap);
+  stage_soft_tile(t, offsets, l0, nlists, cap, sx, x, (T*)nullptr, (const T*)nullptr);
   const long long total = t.loc[t.count];
-  if (t.mapped) {
-    stage_elements(sx, x + t.base, total);
-    __syncthreads();
-  }
   const T* xs = t.mapped ? sx : x + t.base;
   const int r = threadIdx.x;
   if (r < t.count) {  // per-list max and sum of exp(x - max)
@@ -240,13 +221,9 @@ __global__ void __launch_bounds__(kSoftThreads)
   __shared__ T s_sum[kSoftLists];
   __shared__ T s_dot[kSoftLists];
   const long long l0 = (long long)blockIdx.x * kSoftLists;
-  stage_soft_tile(t, offsets, l0, nlists, cap);
-  const long long total = t.loc[t.count];
   const T* src = ysaved ? ysaved : x;
-  if (t.mapped) {
-    stage_elements2(sa, src + t.base, sg, gy + t.base, total);
-    __syncthreads();
-  }
+  stage_soft_tile(t, offsets, l0, nlists, cap, sa, src, sg, gy);
+  const long long total = t.loc[t.count];
   const T* as = t.mapped ? sa : src + t.base;
   const T* gs = t.mapped ? sg : gy + t.base;
   const int r = threadIdx.x;

@@ -14,6 +14,7 @@
 #include <dlfcn.h>
 
 #include <mutex>
+#include <type_traits>
 
 #include "list_tile.cuh"
 
@@ -32,14 +33,19 @@ inline int map_grid(long long n) {
 // errors: 0 jagged slice's stops[i] < starts[i]; 1 jagged slice's offsets
 // extend beyond its content; 2 stops[i] < starts[i]; 3 stops[i] > len(content);
 // 4 index out of range
-template <class C>
+//
+// With W other than void the kernel also gathers the content at each carry
+// into tocontent (array[index] in one pass; tocarry may then be null).
+template <class C, class W = void>
 __global__ void __launch_bounds__(kTileBlock)
     jagged_apply_kernel(int64_t* __restrict__ tooffsets, int64_t* __restrict__ tocarry,
                         const int64_t* __restrict__ slicestarts,
                         const int64_t* __restrict__ slicestops, long long n,
                         const int64_t* __restrict__ sliceindex, long long sliceinnerlen,
                         const C* __restrict__ fromstarts, const C* __restrict__ fromstops,
-                        long long contentlen, ScanTiles st, uint64_t inv, uint64_t* err) {
+                        long long contentlen, ScanTiles st, uint64_t inv, uint64_t* err,
+                        void* __restrict__ tocontent = nullptr,
+                        const void* __restrict__ content = nullptr) {
   __shared__ TileSmem sm;
   __shared__ long long s_slice[kTileLists];
   __shared__ long long s_start[kTileLists];
@@ -86,7 +92,17 @@ __global__ void __launch_bounds__(kTileBlock)
       return;
     }
     if (idx < 0) idx += count;
-    tocarry[prefix + q] = s_start[r] + idx;
+    const long long at = s_start[r] + idx;
+    if constexpr (std::is_void<W>::value) {
+      tocarry[prefix + q] = at;
+    } else {
+      if (at < 0 || at >= contentlen) {  // a start below zero; the CPU kernel does not check it
+        raise_error(err, inv, 3);
+        return;
+      }
+      static_cast<W*>(tocontent)[prefix + q] = __ldg(static_cast<const W*>(content) + at);
+      if (tocarry) tocarry[prefix + q] = at;
+    }
   });
 }
 
@@ -400,6 +416,43 @@ __global__ void __launch_bounds__(kTileBlock)
 GB_JAGGED_APPLY(awkward_ListArray32_getitem_jagged_apply_64, int32_t)
 GB_JAGGED_APPLY(awkward_ListArrayU32_getitem_jagged_apply_64, uint32_t)
 GB_JAGGED_APPLY(awkward_ListArray64_getitem_jagged_apply_64, int64_t)
+
+// array[index] in one pass: the list-tile apply above with the content
+// gathered at each carry, so the carry is neither written nor read back
+// (tocarry may be null).  The index lists are index[index_offsets[i] ..
+// index_offsets[i+1]) and the lists content[offsets[i] .. offsets[i+1]); the
+// errors are the apply's (invocation index 0).
+GB_EXPORT int awkward_gb300_jagged_index_select(int64_t* tooffsets, void* tocontent,
+                                                int64_t* tocarry, const int64_t* index_offsets,
+                                                const int64_t* index, int64_t indexlen,
+                                                const int64_t* offsets, const void* content,
+                                                int64_t itemsize, int64_t contentlen,
+                                                int64_t nlists, uint64_t* err_code,
+                                                void* stream) {
+  cudaStream_t s = (cudaStream_t)stream;
+  if (itemsize != 1 && itemsize != 2 && itemsize != 4 && itemsize != 8)
+    return (int)cudaErrorInvalidValue;
+  if (nlists <= 0) return (int)cudaMemsetAsync(tooffsets, 0, sizeof(int64_t), s);
+  const long long nt = tile_count(nlists);
+  ScanTiles st;
+  void* base = nullptr;
+  cudaError_t e = scan_tiles_alloc(&st, &base, nt, s);
+  if (e != cudaSuccess) return (int)e;
+#define GB_INDEX_SELECT(W)                                                                     \
+  jagged_apply_kernel<int64_t, W><<<(unsigned)nt, kTileBlock, 0, s>>>(                         \
+      tooffsets, tocarry, index_offsets, index_offsets + 1, nlists, index, indexlen, offsets,  \
+      offsets + 1, contentlen, st, 0, err_code, tocontent, content)
+  switch (itemsize) {
+    case 1: GB_INDEX_SELECT(uint8_t); break;
+    case 2: GB_INDEX_SELECT(uint16_t); break;
+    case 4: GB_INDEX_SELECT(uint32_t); break;
+    default: GB_INDEX_SELECT(uint64_t);
+  }
+#undef GB_INDEX_SELECT
+  e = cudaGetLastError();
+  cudaError_t f = scratch_free(base, s);
+  return (int)(e != cudaSuccess ? e : f);
+}
 
 GB_EXPORT int awkward_ListArray_getitem_jagged_carrylen_64(int64_t* carrylen,
                                                           const int64_t* slicestarts,

@@ -9,7 +9,9 @@ kernels, for CUDA tensors:
   ``awkward_ListArray_getitem_jagged_apply`` (src/awkward/contents/listarray.py:573-616)
   and the content carried (``NumpyArray._carry``);
 * ``getitem_jagged_index`` -- ``array[idx]`` with a jagged int64 index
-  (same apply + carry);
+  (same apply + carry); ``index_select`` does it in one kernel (the apply
+  with the content gathered at each carry), ``mask_select`` the same for
+  ``array[mask]``;
 * ``getitem_inner_range``  -- ``array[..., start:stop:step]`` on the innermost
   list level of a two-level ListOffsetArray:
   ``awkward_ListArray_getitem_next_range_carrylength``, the carry allocation,
@@ -99,6 +101,39 @@ def mask_select(offsets, content, mask, with_carry=False):
     if with_carry:
         return tooffsets, out[:k], carry[:k]
     return tooffsets, out[:k]
+
+
+def index_select(offsets, content, index_offsets, index, with_carry=False):
+    """array[idx] with a jagged int64 index in one pass
+    (awkward_gb300_jagged_index_select): the new offsets, the gathered
+    content and, with `with_carry`, the carry -- the same outputs as
+    getitem_jagged_index without writing and re-reading the carry.  Errors
+    are jagged_apply's, raised as ValueError."""
+    from ._messages import messages
+
+    n = offsets.numel() - 1
+    k = index.numel()
+    tooffsets = torch.empty(n + 1, dtype=torch.int64, device=offsets.device)
+    out = torch.empty(max(k, 1), dtype=content.dtype, device=content.device)
+    carry = torch.empty(max(k, 1), dtype=torch.int64, device=offsets.device) if with_carry else None
+    # a one-element stand-in keeps the pointers valid when the content is empty
+    src = content if content.numel() > 0 else torch.zeros(1, dtype=content.dtype,
+                                                          device=content.device)
+    err = _err_word(offsets.device)
+    rc = _abi.ext_cfunc("awkward_gb300_jagged_index_select")(
+        tooffsets.data_ptr(), out.data_ptr(), carry.data_ptr() if with_carry else None,
+        index_offsets.data_ptr(), index.data_ptr(), k, offsets.data_ptr(), src.data_ptr(),
+        content.element_size(), content.numel(), n, err.data_ptr(), _stream(offsets))
+    if rc != 0:
+        raise RuntimeError(f"awkward_gb300_jagged_index_select: cudaError {rc}")
+    word = int(err.item()) & ((1 << 64) - 1)
+    if word != (1 << 64) - 1:
+        msg = messages("awkward_ListArray_getitem_jagged_apply")[word & 255]
+        raise ValueError(f"{msg} in compiled CUDA code (awkward_gb300_jagged_index_select)")
+    m = int(tooffsets[-1].item()) if n > 0 else 0
+    if with_carry:
+        return tooffsets, out[:m], carry[:m]
+    return tooffsets, out[:m]
 
 
 def jagged_apply(offsets, index_offsets, index, contentlen):

@@ -436,6 +436,14 @@ def measure_c2(be, dev, reps, warmup, n_lists=10_000_000):
         k_apply(i_too, i_carry, i_ist, i_isp, n_lists, idx, Ki, starts, stops, E)
         f_take(i_out.data_ptr(), x.data_ptr(), 4, i_carry.data_ptr(), Ki, E, 0, err.data_ptr(), sp)
 
+    f_isel = _abi.ext_cfunc("awkward_gb300_jagged_index_select")
+    j_too = torch.empty(n_lists + 1, dtype=torch.int64, device=dev)
+    j_out = torch.empty(Ki, dtype=torch.float32, device=dev)
+
+    def index_one_pass():
+        f_isel(j_too.data_ptr(), j_out.data_ptr(), None, ioff.data_ptr(), idx.data_ptr(), Ki,
+               off.data_ptr(), x.data_ptr(), 4, E, n_lists, err.data_ptr(), sp)
+
     Lo = torch.poisson(torch.full((n_lists,), 4.0, device=dev), generator=gen).to(torch.int64)
     ninner = int(Lo.sum().item())
     Li = torch.poisson(torch.full((ninner,), 6.0, device=dev), generator=gen).to(torch.int64)
@@ -471,9 +479,13 @@ def measure_c2(be, dev, reps, warmup, n_lists=10_000_000):
         # one pass: mask and offsets read, the content read once, new offsets and
         # the selected content written
         "mask_one_pass": E + 8 * (N + 1) + 4 * E + 8 * (N + 1) + 4 * Km,
+        # one pass: index offsets, offsets and the index read, the content gathered
+        # once, new offsets and the gathered content written (no carry)
+        "index_one_pass": 24 * (N + 1) + 8 * Ki + 4 * Ki + 4 * Ki,
     }
     for name, fn, nl in (("mask", mask_chain, N), ("index", index_chain, N),
-                         ("range", range_chain, N), ("mask_one_pass", mask_one_pass, N)):
+                         ("range", range_chain, N), ("mask_one_pass", mask_one_pass, N),
+                         ("index_one_pass", index_one_pass, N)):
         for _ in range(max(warmup, 3)):
             fn()
         be.synchronize()
@@ -486,6 +498,8 @@ def measure_c2(be, dev, reps, warmup, n_lists=10_000_000):
     res["range"]["kernels"] = "next_range_carrylength + next_range + take (float32)"
     res["mask_one_pass"]["kernels"] = ("awkward_gb300_jagged_mask_select: array[mask] in one "
                                        "kernel (same offsets and content as the chain)")
+    res["index_one_pass"]["kernels"] = ("awkward_gb300_jagged_index_select: array[idx] in one "
+                                        "kernel (same offsets and content as the chain)")
     res["sizes"] = {"lists": N, "elements": E, "selected": Km, "indices": Ki,
                     "inner_lists": ninner, "inner_elements": E2, "range_kept": Kr}
     return res

@@ -735,11 +735,15 @@ int awkward_ListArray64_getitem_jagged_apply_64_noalloc(int64_t* tooffsets, int6
  *   jagged_mask_select: array[mask] in one pass -- the new offsets, the
  *     selected content (itemsize 1, 2, 4 or 8) and optionally the carry
  *     (NULL to skip), without the local index of the chain;
+ *   jagged_index_select: array[index] with a jagged int64 index in one pass
+ *     -- jagged_apply with the content gathered at each carry (itemsize 1, 2,
+ *     4 or 8; tocarry NULL to skip), errors as jagged_apply's;
  *   take: out[i] = content[carry[i]] for itemsize 1, 2, 4 or 8 bytes
  *     (NumpyArray._carry); a carry outside [0, contentlen) sets err_code to
  *     invocation_index*256 + 0 ("index out of range"). */
 int awkward_gb300_jagged_mask_to_index(int64_t* tooffsets, int64_t* toindex, const uint8_t* mask, const int64_t* offsets, int64_t nlists, uint64_t* err_code, void* stream);
 int awkward_gb300_jagged_mask_select(int64_t* tooffsets, void* tocontent, int64_t* tocarry, const uint8_t* mask, const int64_t* offsets, const void* content, int64_t itemsize, int64_t nlists, uint64_t* err_code, void* stream);
+int awkward_gb300_jagged_index_select(int64_t* tooffsets, void* tocontent, int64_t* tocarry, const int64_t* index_offsets, const int64_t* index, int64_t indexlen, const int64_t* offsets, const void* content, int64_t itemsize, int64_t contentlen, int64_t nlists, uint64_t* err_code, void* stream);
 int awkward_gb300_take(void* out, const void* content, int64_t itemsize, const int64_t* carry, int64_t n, int64_t contentlen, uint64_t invocation_index, uint64_t* err_code, void* stream);
 
 /* ---- backward kernels of differentiable jagged operations (torch.autograd

@@ -313,3 +313,52 @@ def test_one_pass_mask_select_no_elements(n):
     so, sc, scarry = jagged.mask_select(doff, dx, dm, with_carry=True)
     assert torch.equal(so, torch.zeros(n + 1, dtype=torch.int64, device="cuda"))
     assert sc.numel() == 0 and scarry.numel() == 0
+
+
+@pytest.mark.parametrize("variant", ["poisson", "base", "long_list", "half_empty"])
+@pytest.mark.parametrize("dt", [np.uint8, np.int16, np.float32, np.float64])
+def test_one_pass_index_select_equals_the_chain(variant, dt):
+    """array[idx] in one pass gives the chain's offsets, carry and content, bit for bit
+    (negative indices included)."""
+    import torch
+
+    from awkward_gb300 import jagged
+
+    extra = np.array([100_000]) if variant == "long_list" else None
+    pe = 0.5 if variant == "half_empty" else 0.01
+    rng, L, off, x, _mask = _case(20_000, 9, base=5 if variant == "base" else 0, extra=extra,
+                                  pe=pe)
+    ioff, idx = _index_case(rng, L)
+    xs = (x * 3).astype(dt) if np.dtype(dt).kind != "f" else x.astype(dt)
+    d = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    doff, dx, dio, dix = d(off), d(xs), d(ioff), d(idx)
+    so, sc, scarry = jagged.index_select(doff, dx, dio, dix, with_carry=True)
+    co, ccarry = jagged.jagged_apply(doff, dio, dix, dx.numel())
+    cc = jagged.take(dx, ccarry)
+    torch.testing.assert_close(so, co, rtol=0, atol=0)
+    torch.testing.assert_close(scarry, ccarry, rtol=0, atol=0)
+    assert torch.equal(sc.view(torch.uint8), cc.view(torch.uint8))
+    so2, sc2 = jagged.index_select(doff, dx, dio, dix)
+    assert torch.equal(so2, so) and torch.equal(sc2.view(torch.uint8), sc.view(torch.uint8))
+
+
+def test_one_pass_index_select_errors_and_empty():
+    import torch
+
+    from awkward_gb300 import jagged
+
+    off = torch.tensor([0, 2, 5], dtype=torch.int64, device="cuda")
+    x = torch.arange(5, dtype=torch.float32, device="cuda")
+    ioff = torch.tensor([0, 1, 2], dtype=torch.int64, device="cuda")
+    with pytest.raises(ValueError, match="index out of range"):
+        jagged.index_select(off, x, ioff, torch.tensor([0, 3], dtype=torch.int64, device="cuda"))
+    so, sc = jagged.index_select(off, x, ioff, torch.tensor([-1, -3], dtype=torch.int64,
+                                                            device="cuda"))
+    assert so.tolist() == [0, 1, 2] and sc.tolist() == [1.0, 2.0]
+    # no lists, and lists with no index entries
+    empty = torch.zeros(0, dtype=torch.int64, device="cuda")
+    so, sc = jagged.index_select(torch.zeros(1, dtype=torch.int64, device="cuda"), x[:0],
+                                 torch.zeros(1, dtype=torch.int64, device="cuda"), empty)
+    assert so.tolist() == [0] and sc.numel() == 0
+    so, sc = jagged.index_select(off, x, torch.zeros(3, dtype=torch.int64, device="cuda"), empty)
+    assert so.tolist() == [0, 0, 0] and sc.numel() == 0
