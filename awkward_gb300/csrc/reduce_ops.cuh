@@ -25,11 +25,12 @@
 namespace gb {
 
 // This GPU executes float64 arithmetic AND comparisons on a narrow pipe
-// (about 1/64 of float32), so the float64 reducers below never use it per
-// element: comparisons go through an integer total-order key and sums through
-// a fixed-point accumulator on the integer pipe (addend bits below the
-// anchor's unit truncated, the total rounded once: within n*eps*sum|x| of the
-// exact sum).
+// (about 1/64 of float32), so the float64 reducers below keep most per-element
+// work off it: comparisons go through an integer total-order key, and sums
+// split each short run between the float64 unit (even positions, one add
+// each) and a fixed-point accumulator on the integer pipe (odd positions;
+// addend bits below the anchor's unit truncated, the total rounded once:
+// within n*eps*sum|x| of the exact sum).
 template <class T>
 __device__ __forceinline__ bool is_nan(T v) {
   if constexpr (std::is_same<T, double>::value) {
