@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "list_tile.cuh"
+#include "mask_select.cuh"
 #include "reduce_ops.cuh"
 
 using namespace gb;
@@ -137,13 +138,13 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// array[mask] and count for every list tile of every array.
-__global__ void __launch_bounds__(kTileBlock)
+// array[mask] and count for every list tile of every array (mask_select_tile;
+// tiles are claimed from one ticket over all arrays' tiles in order).
+__global__ void __launch_bounds__(kTileBlock, 8)
     batch_select_kernel(const BatchArray* __restrict__ arrays, int narrays,
                         const long long* __restrict__ tile_base, unsigned long long* ticket,
                         unsigned long long* status, uint64_t* err) {
-  __shared__ TileSmem sm;
-  __shared__ long long loc[kTileLists + 1];
+  __shared__ MaskSelectSmem sm;
   __shared__ int s_arr;
   if (threadIdx.x == 0) {
     const long long g = (long long)atomicAdd(ticket, 1ull);
@@ -153,61 +154,17 @@ __global__ void __launch_bounds__(kTileBlock)
       if (tile_base[mid] <= g) lo = mid;
       else hi = mid;
     }
-    sm.tile = g - tile_base[lo];
+    sm.tile.tile = g - tile_base[lo];
     s_arr = lo;
   }
   __syncthreads();
-  const long long tile = sm.tile;
+  const long long tile = sm.tile.tile;
   const BatchArray& A = arrays[s_arr];
   ScanTiles st;
   st.ticket = ticket;
   st.status = status + A.tile0;
-  const long long l0 = tile * kTileLists;
-  const long long rem = A.nlists - l0;
-  const int count = (int)(rem < kTileLists ? rem : kTileLists);
-  const long long base = __ldg(A.offsets + l0);
-  for (int i = threadIdx.x; i <= kTileLists; i += kTileBlock) {
-    const int k = i < count ? i : count;
-    loc[i] = __ldg(A.offsets + l0 + k) - base;
-  }
-  __syncthreads();
-  long long c[kTileLPT];
-#pragma unroll
-  for (int r = 0; r < kTileLPT; r++) {
-    const int li = threadIdx.x * kTileLPT + r;
-    long long n = 0;
-    if (li < count) {
-      for (long long j = base + loc[li]; j < base + loc[li + 1]; j++) n += A.mask[j] != 0;
-      A.out_count[l0 + li] = loc[li + 1] - loc[li];
-    }
-    c[r] = n;
-  }
-  const long long prefix = tile_scan(sm, st, tile, c, 0, err);
-  for (int li = threadIdx.x; li < count; li += kTileBlock) A.sel_offsets[l0 + li] = prefix + sm.loc[li];
-  if (l0 + count == A.nlists && threadIdx.x == 0) A.sel_offsets[A.nlists] = prefix + sm.total;
-  constexpr int kWarps = kTileBlock / 32;
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const long long total = loc[count];
-  const long long qa = total * warp / kWarps, qb = total * (warp + 1) / kWarps;
-  if (qa >= qb) return;
-  int lo = 0, hi = count;
-  while (hi - lo > 1) {
-    const int mid = (lo + hi) >> 1;
-    if (loc[mid] <= qa) lo = mid;
-    else hi = mid;
-  }
-  long long before = 0;
-  for (long long q = loc[lo] + lane; q < qa; q += 32) before += A.mask[base + q] != 0;
-#pragma unroll
-  for (int d = 16; d > 0; d >>= 1) before += __shfl_xor_sync(0xffffffffu, before, d);
-  long long run = prefix + sm.loc[lo] + before;
-  for (long long g = qa; g < qb; g += 32) {
-    const long long q = g + lane;
-    const bool m = q < qb && A.mask[base + q] != 0;
-    const unsigned b = __ballot_sync(0xffffffffu, m);
-    if (m) A.sel_content[run + __popc(b & ((1u << lane) - 1u))] = A.x[base + q];
-    run += __popc(b);
-  }
+  mask_select_tile<double>(sm, tile, A.nlists, A.offsets, A.mask, A.x, A.sel_offsets,
+                           A.sel_content, nullptr, A.out_count, st, err);
 }
 
 struct Plan {
