@@ -30,6 +30,7 @@ next ``synchronize()`` raises that code's message (code 32: the library's
 
 from __future__ import annotations
 
+import collections
 import os
 
 import numpy as np
@@ -105,6 +106,27 @@ class _StreamContext:
             self.err.copy_(torch.where((self.err < 0) | (self.err > w), w, self.err))
 
 
+# Device arrays of row pointers (the int64_t** arguments), by device and
+# addresses: uploading one is a blocking host-to-device copy, so a repeated
+# call with the same rows reuses the array (it holds nothing but those
+# addresses, so a cached array is right whatever tensors now live there).
+_PTR_ARRAYS: collections.OrderedDict = collections.OrderedDict()
+_PTR_ARRAYS_MAX = 256
+
+
+def _pointer_array(dev, addresses):
+    key = (dev.index, addresses)
+    arr = _PTR_ARRAYS.get(key)
+    if arr is None:
+        arr = torch.tensor(list(addresses) or [0], dtype=torch.int64, device=dev)
+        _PTR_ARRAYS[key] = arr
+        if len(_PTR_ARRAYS) > _PTR_ARRAYS_MAX:
+            _PTR_ARRAYS.popitem(last=False)
+    else:
+        _PTR_ARRAYS.move_to_end(key)
+    return arr
+
+
 class GB300Kernel:
     """One specialization, callable with the spec's arguments."""
 
@@ -147,7 +169,7 @@ class GB300Kernel:
                     raise TypeError(f"{self.name}: rows of {an} must be CUDA {TORCH_OF_C[base]} tensors")
                 device = t.device
             dev = device if device is not None else torch.device("cuda", torch.cuda.current_device())
-            ptrs = torch.tensor([t.data_ptr() for t in rows] or [0], dtype=torch.int64, device=dev)
+            ptrs = _pointer_array(dev, tuple(t.data_ptr() for t in rows))
             keep.extend(rows)
             keep.append(ptrs)
             cargs.append(ptrs.data_ptr())
