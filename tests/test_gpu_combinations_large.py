@@ -139,3 +139,32 @@ def test_combinations_pairs_full_size_properties():
     inc = (a[1:] > a[:-1]) | ((a[1:] == a[:-1]) & (b[1:] > b[:-1]))
     assert bool(inc[same].all())
     assert ti.tolist() == [P, P]
+
+
+def test_row_pointer_arrays_are_reused_and_rebuilt():
+    """The int64_t** argument's device array is cached by the rows' addresses:
+    the same rows reuse it, other rows get their own, and calls through either
+    write into the rows they name."""
+    import torch
+
+    import awkward_gb300
+    from awkward_gb300 import kernel_table
+
+    be = awkward_gb300.backend()
+    k = be.by_name("awkward_ListArray64_combinations_64")
+    off = torch.tensor([0, 3, 5], dtype=torch.int64, device="cuda")
+    st, sp = off[:-1].contiguous(), off[1:].contiguous()
+    ti = torch.empty(2, dtype=torch.int64, device="cuda")
+    fi = torch.zeros(2, dtype=torch.int64, device="cuda")
+    rows_a = [torch.full((4,), -1, dtype=torch.int64, device="cuda") for _ in range(2)]
+    rows_b = [torch.full((4,), -1, dtype=torch.int64, device="cuda") for _ in range(2)]
+    dev = torch.device("cuda", torch.cuda.current_device())
+    k(rows_a, ti, fi, 2, False, st, sp, 2)
+    arr = kernel_table._pointer_array(dev, tuple(t.data_ptr() for t in rows_a))
+    k(rows_a, ti, fi, 2, False, st, sp, 2)
+    assert kernel_table._pointer_array(dev, tuple(t.data_ptr() for t in rows_a)) is arr
+    k(rows_b, ti, fi, 2, False, st, sp, 2)
+    be.synchronize()
+    expect = [[0, 0, 1, 3], [1, 2, 2, 4]]
+    assert [r.tolist() for r in rows_a] == expect and [r.tolist() for r in rows_b] == expect
+    assert arr.tolist() == [t.data_ptr() for t in rows_a]
