@@ -32,9 +32,6 @@ __device__ __forceinline__ void raise_error(uint64_t* err, uint64_t inv, int cod
   atomicMin(reinterpret_cast<unsigned long long*>(err),
             static_cast<unsigned long long>(inv * (1ull << GB_ERROR_BITS) + (uint64_t)code));
 }
-__device__ __forceinline__ bool error_pending(const uint64_t* err) {
-  return *reinterpret_cast<const volatile uint64_t*>(err) != GB_NO_ERROR;
-}
 
 // ----------------------------------------------------------------- scratch
 // Stream-ordered allocation from a per-device pool owned by the library.
@@ -52,15 +49,6 @@ __device__ __forceinline__ V shfl_up(V v, int delta) {
   u.v = v;
 #pragma unroll
   for (int i = 0; i < W; i++) u.w[i] = __shfl_up_sync(0xffffffffu, u.w[i], delta);
-  return u.v;
-}
-template <class V>
-__device__ __forceinline__ V shfl_down(V v, int delta) {
-  constexpr int W = sizeof(V) / 4;
-  union U { V v; uint32_t w[W]; } u;
-  u.v = v;
-#pragma unroll
-  for (int i = 0; i < W; i++) u.w[i] = __shfl_down_sync(0xffffffffu, u.w[i], delta);
   return u.v;
 }
 template <class V>

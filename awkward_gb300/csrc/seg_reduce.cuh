@@ -133,11 +133,6 @@ __device__ __forceinline__ typename Op::Acc warp_allreduce(const Op& op, typenam
   return a;
 }
 
-template <class T>
-__device__ __forceinline__ T ld_ro(const T* p) {
-  return __ldg(p);
-}
-
 // Reduction of one run of a list by a group of G lanes (defined, with its
 // per-reducer overloads, in reduce_ops.cuh).
 template <int G, class Op>
